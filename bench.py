@@ -1,0 +1,368 @@
+"""Benchmark: IVIM voxel fits/s of the batched LM fitter on GB300.
+
+Workload (default): plain LM at scale - IVIM bi-exponential, 4 parameters,
+b = {0,10,20,50,100,200,400,600,800,1000} s/mm^2, 256x256x128 = 8,388,608
+voxels, fp32 state with the GMW81 solve and gain-ratio test in fp64, at most
+100 iterations per voxel, constant initialisation [max S, 0.1, 1e-2, 1e-3],
+seeded synthetic signals (uniform true parameters, Rician noise at SNR 50).
+
+One step = one full fit of every voxel: the fitter state is reset from the
+initial parameters and run(100) is called. Inputs (335 MB of signals) are
+larger than L2 (129 MB), so no L2 flush is needed between steps.
+
+Reported (one JSON line from rank 0):
+  value        fits/s with inputs resident in HBM (whole job over ranks)
+  e2e          fits/s through the public API from pinned host buffers,
+               host->device copies of signals and initial parameters and the
+               device->host read of fitted parameters and status inside the
+               timed region
+  roofline     HBM roofline of the LM kernel: algorithmic bytes
+               (4M + 4P + 1 per voxel: signals in, parameters and status out)
+               over the kernel's event-timed duration, against the measured
+               copy bandwidth in MEASURED_PEAKS.json
+  cpu_baseline the CPU oracle (the reference algorithm in fp32) on a bounded
+               sample on all host cores
+  accuracy     median relative error of the fitted maps against the all-FP64
+               GPU fitter (same LM, same initialisation)
+
+`--impl reference` times the reference's CPU implementation instead (its own
+generated kernel built for the host when available, else the CPU oracle in the
+reference's fp32 arithmetic) on all host threads, one bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+M_IVIM10 = 10
+P_IVIM = 4
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            pk = json.load(f)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.gpu)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def cpu_sample(iters: int, target_s: float, dtype_mode: str = "reference", min_voxels: int = 16384):
+    """Time the CPU reference implementation on a bounded IVIM-10 sample.
+
+    Uses the reference's generated kernel built for the host (oracle/_ref)
+    when present, else the CPU oracle in the reference's fp32 arithmetic. The
+    sample doubles until one run takes at least target_s/4 seconds, then the
+    last size is timed once. Returns (fits_per_s, kind, cores, sample_text).
+    """
+    from oracle import OracleModel, RefIVIM, ref_available
+    from pycompute_gb300 import synth
+
+    w = synth.ivim()
+    cores = os.cpu_count() or 1
+    if ref_available(M_IVIM10):
+        impl, kind = RefIVIM(M_IVIM10), "reference"
+        run = lambda p, d, i, lb, ub, prot: impl.lm_run(p, prot, d, lb, ub, iters)  # noqa: E731
+    else:
+        impl, kind = OracleModel(w.expr, w.pars, w.consts), "port"
+        impl.set_threads(cores)
+        run = lambda p, d, i, lb, ub, prot: impl.lm_run(p, prot, d, lb, ub, iters)  # noqa: E731
+    n = min_voxels
+    while True:
+        true, data, init, lb, ub, prot = w.generate(n, seed=7)
+        p = init.copy()
+        t0 = time.perf_counter()
+        run(p, data, init, lb, ub, prot)
+        el = time.perf_counter() - t0
+        if el >= target_s / 4 or n >= (1 << 22):
+            break
+        n *= 2 if el > 0.05 else 8
+    sample = (f"{n} IVIM-10 voxels x {iters} iterations ({'reference generated kernel' if kind == 'reference' else 'fp32 oracle port'}, "
+              f"{cores} threads), {el:.2f} s")
+    return n / el, kind, cores, sample
+
+
+def run_reference_arm(args):
+    ws, rank, local = _dist()
+    if rank != 0:
+        return 0
+    vals = []
+    for s in range(args.warmup + args.steps):
+        v, kind, cores, sample = cpu_sample(args.iters, target_s=args.cpu_seconds, min_voxels=16384)
+        if s >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": "IVIM voxel fits/s", "value": value, "unit": "fits/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded IVIM-10, Rician SNR 50)",
+        "config": {"workload": "ivim10_plain_lm_cpu_sample", "iters": args.iters},
+        "cpu_baseline": {"value": value, "unit": "fits/s", "cores": cores, "kind": kind, "sample": sample},
+        "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--voxels", type=int, default=256 * 256 * 128)
+    ap.add_argument("--iters", type=int, default=100)
+    ap.add_argument("--solve", default="f64", choices=["f64", "f32"])
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    import torch.distributed as dist
+
+    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, parity, synth
+
+    ws, rank, local = _dist()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    w = synth.ivim()
+    N = args.voxels
+    # each rank fits its own shard (weak scaling): seeds differ per rank
+    true, data, init, lb, ub, prot = w.generate(N, seed=1000 + rank)
+    solve = torch.float64 if args.solve == "f64" else torch.float32
+    expr = Expr(w.expr, w.pars, w.consts)
+    solm = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32, solve_dtype=solve)
+
+    data_d = torch.from_numpy(data).to(dev)
+    init_d = torch.from_numpy(init).to(dev)
+    prot_d = torch.from_numpy(prot).to(dev)
+    lb_d = torch.from_numpy(lb).to(dev)
+    ub_d = torch.from_numpy(ub).to(dev)
+    pars_d = init_d.clone()
+    solm.setup(pars_d, prot_d, data_d, lb_d, ub_d)
+    stream = torch.cuda.current_stream()
+
+    def reset():
+        pars_d.copy_(init_d)
+        solm.lam_t.fill_(5.0)
+        solm.step_type_t.fill_(1)
+        solm.f_t.zero_()
+        solm.iters_t.zero_()
+
+    # ---- device-resident timing -------------------------------------------
+    for _ in range(args.warmup):
+        reset()
+        solm.run(args.iters, block=args.block)
+    torch.cuda.synchronize()
+    k_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    k_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_start.record(stream)
+        for s in range(args.steps):
+            reset()
+            k_start[s].record(stream)
+            solm.run(args.iters, block=args.block)
+            k_end[s].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    step_ms = t_start.elapsed_time(t_end) / args.steps
+    kern_ms = statistics.mean(k_start[s].elapsed_time(k_end[s]) for s in range(args.steps))
+    if ws > 1:
+        t = torch.tensor([step_ms, kern_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        step_ms, kern_ms = float(t[0]), float(t[1])
+    fitted = pars_d.cpu().numpy()
+    st = solm.step_type_t.cpu().numpy()[0]
+    its = solm.iters_t.cpu().numpy()[0].astype(np.int64)
+
+    # ---- end to end through the public API from pinned host buffers -------
+    data_h = torch.from_numpy(data).pin_memory()
+    init_h = torch.from_numpy(init).pin_memory()
+    out_pars_h = torch.empty_like(init_h).pin_memory()
+    out_st_h = torch.empty((1, N), dtype=torch.int8).pin_memory()
+    data_e = torch.empty_like(data_d)
+    pars_e = torch.empty_like(init_d)
+    solm_e = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32, solve_dtype=solve)
+
+    def e2e_step():
+        data_e.copy_(data_h, non_blocking=True)
+        pars_e.copy_(init_h, non_blocking=True)
+        solm_e.setup(pars_e, prot_d, data_e, lb_d, ub_d)
+        solm_e.run(args.iters, block=args.block)
+        out_pars_h.copy_(pars_e, non_blocking=True)
+        out_st_h.copy_(solm_e.step_type_t, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    e_start = torch.cuda.Event(enable_timing=True)
+    e_end = torch.cuda.Event(enable_timing=True)
+    e_start.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e_end.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e_start.elapsed_time(e_end) / args.steps
+    if ws > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t[0])
+    assert np.array_equal(out_pars_h.numpy(), fitted), "e2e result differs from the device-resident run"
+    h2d = data.nbytes + init.nbytes
+    d2h = init.nbytes + N
+
+    # ---- accuracy against the all-FP64 fitter (untimed) -------------------
+    acc = None
+    if not args.no_fp64_check:
+        solm64 = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float64)
+        p64 = init_d.double()
+        solm64.setup(p64, prot_d.double(), data_d.double(), lb_d.double(), ub_d.double())
+        t0 = time.perf_counter()
+        solm64.run(args.iters)
+        torch.cuda.synchronize()
+        t64 = time.perf_counter() - t0
+        rep = parity.compare_params(fitted, p64.cpu().numpy())
+        acc = {"vs": "all-FP64 GPU fitter, same LM and init", "median_rel_err": rep["median_rel"],
+               "frac_voxels_gt_1e-4": rep["frac_gt_1e-4"], "per_param_median": rep["per_param_median"],
+               "flags_agree": parity.flags_agree(st, solm64.step_type_t.cpu().numpy()),
+               "fp64_fit_s": round(t64, 3)}
+        del p64, solm64
+
+    # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        v, kind, cores, sample = cpu_sample(args.iters, target_s=args.cpu_seconds)
+        cpu = {"value": v, "unit": "fits/s", "cores": cores, "kind": kind, "sample": sample}
+
+    if rank == 0:
+        hbm, peak_kind = _peaks()
+        bytes_per_voxel = 4 * M_IVIM10 + 4 * P_IVIM + 1
+        achieved = bytes_per_voxel * N / (kern_ms / 1e3) / 1e9
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "lm_ivim10_traffic.json")
+        if os.path.exists(tf):
+            with open(tf) as f:
+                tr = json.load(f)
+            traffic = tr["dram_bytes_per_voxel"] * N
+        value = ws * N / (step_ms / 1e3)
+        line = {
+            "metric": "IVIM voxel fits/s (plain LM, 100 iters max)", "value": value, "unit": "fits/s",
+            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 (f64 GMW81 solve + gain ratio)" if args.solve == "f64" else "f32",
+            "data": "synthetic (seeded IVIM-10, Rician SNR 50)",
+            "config": {"workload": "ivim10_plain_lm_8.4M", "voxels_per_gpu": N, "ndata": M_IVIM10,
+                       "nparam": P_IVIM, "iters": args.iters, "solve": args.solve, "init": "constant",
+                       "l2": "inputs larger than L2 (335 MB signals)", "parallelism": f"voxel shards x{ws}"},
+            "e2e": {"value": ws * N / (e2e_ms / 1e3), "unit": "fits/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_voxel": bytes_per_voxel,
+                         "note": "iterative per-voxel solver: FP64/FP32 issue bound, not HBM bound"},
+            "kernel_ms": kern_ms,
+            "fit_stats": {"mean_iters": float(its.mean()), "converged_frac": float(np.mean(st == 0)),
+                          "voxel_iters_per_s": float(its.sum()) * ws / (kern_ms / 1e3)},
+            "accuracy": acc,
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

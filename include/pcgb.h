@@ -1,0 +1,135 @@
+/*
+ * pcgb.h - C ABI of the GB300 batched Levenberg-Marquardt fitter.
+ *
+ * The reference (turbotage/pycompute) has no native library: its Python
+ * classes render CUDA C from Jinja templates, compile it with NVRTC through
+ * cupy.RawModule and launch the kernels directly. Each entry point below
+ * replaces one of those Python-side operations; the comment on each names the
+ * reference code it stands for (paths relative to the pycompute tree).
+ *
+ * Conventions
+ *  - All array arguments are device pointers to C-contiguous structure-of-
+ *    arrays buffers with the voxel index fastest, exactly the reference's
+ *    layouts: params (P, N), data (M, N), consts (C*M, N), bounds (P, N),
+ *    lam / f (N), step_type int8 (N).
+ *  - "dtype" is 0 for float32 and 1 for float64 buffers.
+ *  - Calls are asynchronous on the given cudaStream_t (passed as void*;
+ *    NULL = legacy default stream), like the reference's launches on CuPy's
+ *    current stream.
+ *  - Every function returns 0 on success and a negative errno-style code on
+ *    failure; pcgb_last_error() then describes the failure (per host thread).
+ *    Nothing aborts, traps or prints.
+ *  - A pcgb_fitter is not thread-safe; use one per host thread or lock.
+ */
+#ifndef PCGB_H
+#define PCGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PCGB_OK 0
+#define PCGB_EINVAL (-22)
+#define PCGB_ENOMEM (-12)
+#define PCGB_ECOMPILE (-1001)
+#define PCGB_ECUDA (-1002)
+#define PCGB_ERANGE (-34)
+
+#define PCGB_DTYPE_F32 0
+#define PCGB_DTYPE_F64 1
+
+typedef struct pcgb_fitter pcgb_fitter;
+
+/* Library version string and the maximum sizes compiled into it. */
+const char* pcgb_version(void);
+int pcgb_max_params(void);
+int pcgb_max_protocol(void);
+
+/* Description of the last failure on this host thread ("" if none). */
+const char* pcgb_last_error(void);
+
+/*
+ * Build a fitter program for one model, one protocol length and one precision.
+ * Replaces SecondOrderLevenbergMarquardt.__init__/build (lsqnonlin.py:949-975,
+ * 1013-1025): code generation of the orchestration kernel and its device
+ * functions, cudap.code_gen_walking (cuda_program.py:193-203) and
+ * cp.RawModule(code=...) (lsqnonlin.py:1019-1020).
+ *   model_source  the generated model struct (m, dm/dp, d2m/dp2)
+ *   model_struct  its type name
+ *   nparam/nconst/ndata  P, C (constants per sample) and M
+ *   dtype         state/accumulation type (PCGB_DTYPE_F32 or _F64)
+ *   solve_dtype   type of the GMW81 solve and gain-ratio test
+ *   cache_dir     directory for compiled cubins keyed by source hash, or NULL
+ * The program is compiled with NVRTC for sm_103a and loaded on the current
+ * device.
+ */
+int pcgb_fitter_create(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata,
+                       int dtype, int solve_dtype, const char* cache_dir, pcgb_fitter** out);
+
+/*
+ * Compile (and cache) the same program without loading it: no GPU is needed.
+ * The compiler log (ptxas register and spill report) is copied into
+ * log_buf (truncated to log_len bytes). Used by the build step to check the
+ * kernel templates and by tooling; it has no reference counterpart.
+ */
+int pcgb_fitter_compile(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata,
+                        int dtype, int solve_dtype, const char* cache_dir, char* log_buf, size_t log_len);
+
+/* Release the program (cudaLibraryUnload). */
+int pcgb_fitter_destroy(pcgb_fitter* fitter);
+
+/* Compiler log of the last build (register use from ptxas -v), "" if cached. */
+const char* pcgb_fitter_log(const pcgb_fitter* fitter);
+
+/*
+ * Run `iters` LM iterations on N voxels in one launch.
+ * Replaces SecondOrderLevenbergMarquardt.run (lsqnonlin.py:1058-1073): the
+ * host loop of `iters` launches of k_second_order_levenberg_marquardt_*
+ * (kernel arguments lsqnonlin.py:991-994) and the first_f / last_f copies.
+ *   consts        (C*M, N) per voxel when consts_stride == N; when
+ *                 consts_stride == 0 the protocol is shared by all voxels and
+ *                 is taken from protocol_host (C*M host values) instead
+ *   lower/upper   (P, N) when bounds_stride == N; shared bounds from
+ *                 lb_host / ub_host (P host values) when bounds_stride == 0
+ *   params        (P, N) initial values in, fitted values out
+ *   step          (P, N) last step out, or NULL
+ *   lam           (N) damping in/out (the reference starts it at 5)
+ *   step_type     (N) int8 in/out (1 to start; 0 = converged, else 1/2/4 | 8)
+ *   f             (N) cost at the last evaluated iterate, in/out
+ *   first_f/last_f (N) cost after the first / last iteration of this call
+ *   iters_done    (N) int32 counter incremented by the iterations run, or NULL
+ *   tol, mu, eta, acc, dec  the reference's run() arguments
+ *   block         threads per block (0 = library default)
+ */
+int pcgb_lm_run(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type, void* f,
+                void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host, int block,
+                void* stream);
+
+/*
+ * Accumulating objective f[v] += sum_i (m(p_v; c_i) - d_i)^2, voxels whose
+ * step_type is 0 skipped (step_type may be NULL). Replaces F.run
+ * (lsqnonlin.py:137-145; kernel lsqnonlin.py:160-172).
+ */
+int pcgb_f_run(pcgb_fitter* fitter, const void* params, const void* consts, int64_t consts_stride, const void* data,
+               const int8_t* step_type, void* f, int64_t nprobs, const double* protocol_host, int protocol_len,
+               void* stream);
+
+/*
+ * Batched GMW81 modified-Cholesky solve of packed symmetric (H, N) matrices
+ * (row i, column j <= i) with (P, N) right-hand sides into (P, N) solutions.
+ * Replaces GMW81Solver.run (solver.py:503-510; kernel solver.py:526-563).
+ */
+int pcgb_gmw81_solve(pcgb_fitter* fitter, const void* mat, const void* rhs, void* sol, int64_t nprobs,
+                     void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PCGB_H */

@@ -1,0 +1,80 @@
+"""ctypes binding of libpcgb.so (the C ABI declared in include/pcgb.h).
+
+The library is built in-tree by ``pycompute_gb300.build``. Loading it is
+mandatory: if it is missing or fails to load, every fitter call raises; there
+is no Python or PyTorch fallback for the fitting kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+c_int, c_i64, c_double, c_void_p, c_char_p, c_size_t = (ctypes.c_int, ctypes.c_int64, ctypes.c_double,
+                                                        ctypes.c_void_p, ctypes.c_char_p, ctypes.c_size_t)
+
+# name -> (restype, argtypes); exactly the entry points of include/pcgb.h
+SIGNATURES = {
+    "pcgb_version": (c_char_p, []),
+    "pcgb_max_params": (c_int, []),
+    "pcgb_max_protocol": (c_int, []),
+    "pcgb_last_error": (c_char_p, []),
+    "pcgb_fitter_create": (c_int, [c_char_p, c_char_p, c_int, c_int, c_int, c_int, c_int, c_char_p,
+                                   ctypes.POINTER(c_void_p)]),
+    "pcgb_fitter_compile": (c_int, [c_char_p, c_char_p, c_int, c_int, c_int, c_int, c_int, c_char_p, c_char_p,
+                                    c_size_t]),
+    "pcgb_fitter_destroy": (c_int, [c_void_p]),
+    "pcgb_fitter_log": (c_char_p, [c_void_p]),
+    "pcgb_lm_run": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_double, c_double,
+                            c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                            c_void_p, c_void_p, c_i64, c_int, c_void_p, c_int, c_void_p, c_void_p, c_int,
+                            c_void_p]),
+    "pcgb_f_run": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p,
+                           c_int, c_void_p]),
+    "pcgb_gmw81_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+}
+
+
+class PcgbError(RuntimeError):
+    """A C-ABI call returned an error code."""
+
+    def __init__(self, fn: str, code: int, msg: str):
+        super().__init__(f"{fn} failed ({code}): {msg}")
+        self.code = code
+
+
+def lib(build_if_missing: bool = True):
+    """The loaded library (built first if needed)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_missing:
+            path = _build.build()
+        if not os.path.exists(path):
+            raise RuntimeError(f"native library {path} is missing: run pycompute_gb300.build.build()")
+        L = ctypes.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def check(fn_name: str, rc: int):
+    if rc != 0:
+        msg = lib().pcgb_last_error().decode(errors="replace")
+        raise PcgbError(fn_name, rc, msg)
+
+
+def cache_dir() -> str:
+    d = os.environ.get("PCGB_CACHE_DIR") or os.path.join(_build.BUILD, "jit")
+    os.makedirs(d, exist_ok=True)
+    return d

@@ -1,0 +1,403 @@
+// Device code of the batched second-order Levenberg-Marquardt fitter for
+// sm_103a. The host library compiles it at run time together with one
+// generated model struct (m, dm/dp, d2m/dp2 as straight-line code) and the
+// launch parameters of lm_params.h.
+//
+// One thread owns one voxel for the whole fit: parameters, damping, the
+// packed normal matrix, the data samples and the bounds live in registers;
+// P, H = P(P+1)/2 and the sample count M are compile-time constants, so every
+// loop below unrolls and no array touches local memory. A voxel runs all of
+// its iterations inside one launch and leaves as soon as it converges (the
+// reference relaunches the kernel `iters` times and re-reads its state from
+// global memory each time, pycompute/cuda/lsqnonlin.py:1058-1068).
+//
+// Numerics follow the reference kernel (pycompute/cuda/lsqnonlin.py:823-924)
+// step for step, with two type parameters:
+//   TA  state, residuals, sums over samples, convergence test
+//   TS  GMW81 LDL^T factorisation and solve, gain-ratio test
+// <float, double> is the FP32-bulk / FP64-solve fitter, <float, float> the
+// reference's fp32 arithmetic, <double, double> the all-FP64 oracle run.
+#pragma once
+
+#define PCGB_HD __device__ __forceinline__
+
+PCGB_HD float pcgb_exp(float x) { return expf(x); }
+PCGB_HD double pcgb_exp(double x) { return exp(x); }
+PCGB_HD float pcgb_log(float x) { return logf(x); }
+PCGB_HD double pcgb_log(double x) { return log(x); }
+PCGB_HD float pcgb_sin(float x) { return sinf(x); }
+PCGB_HD double pcgb_sin(double x) { return sin(x); }
+PCGB_HD float pcgb_cos(float x) { return cosf(x); }
+PCGB_HD double pcgb_cos(double x) { return cos(x); }
+PCGB_HD float pcgb_tan(float x) { return tanf(x); }
+PCGB_HD double pcgb_tan(double x) { return tan(x); }
+PCGB_HD float pcgb_asin(float x) { return asinf(x); }
+PCGB_HD double pcgb_asin(double x) { return asin(x); }
+PCGB_HD float pcgb_acos(float x) { return acosf(x); }
+PCGB_HD double pcgb_acos(double x) { return acos(x); }
+PCGB_HD float pcgb_atan(float x) { return atanf(x); }
+PCGB_HD double pcgb_atan(double x) { return atan(x); }
+PCGB_HD float pcgb_sinh(float x) { return sinhf(x); }
+PCGB_HD double pcgb_sinh(double x) { return sinh(x); }
+PCGB_HD float pcgb_cosh(float x) { return coshf(x); }
+PCGB_HD double pcgb_cosh(double x) { return cosh(x); }
+PCGB_HD float pcgb_tanh(float x) { return tanhf(x); }
+PCGB_HD double pcgb_tanh(double x) { return tanh(x); }
+PCGB_HD float pcgb_abs(float x) { return fabsf(x); }
+PCGB_HD double pcgb_abs(double x) { return fabs(x); }
+PCGB_HD float pcgb_erf(float x) { return erff(x); }
+PCGB_HD double pcgb_erf(double x) { return erf(x); }
+PCGB_HD float pcgb_sqrt(float x) { return sqrtf(x); }
+PCGB_HD double pcgb_sqrt(double x) { return sqrt(x); }
+PCGB_HD float pcgb_pow(float x, float y) { return powf(x, y); }
+PCGB_HD double pcgb_pow(double x, double y) { return pow(x, y); }
+
+namespace pcgb {
+
+template <typename T> struct Num;
+template <> struct Num<float> {
+  static PCGB_HD float gmw_eps() { return 2e-7f; }    // solver.py:105
+  static PCGB_HD float damp_floor() { return 1e-4f; } // lsqnonlin.py:275
+  static PCGB_HD float prot(const PcgbLmParams& a, int i) { return a.protocol_f[i]; }
+  static PCGB_HD float slb(const PcgbLmParams& a, int k) { return a.shared_lb_f[k]; }
+  static PCGB_HD float sub(const PcgbLmParams& a, int k) { return a.shared_ub_f[k]; }
+};
+template <> struct Num<double> {
+  static PCGB_HD double gmw_eps() { return 4e-16; }   // solver.py:109
+  static PCGB_HD double damp_floor() { return 1e-4; } // lsqnonlin.py:278
+  static PCGB_HD double prot(const PcgbLmParams& a, int i) { return a.protocol_d[i]; }
+  static PCGB_HD double slb(const PcgbLmParams& a, int k) { return a.shared_lb_d[k]; }
+  static PCGB_HD double sub(const PcgbLmParams& a, int k) { return a.shared_ub_d[k]; }
+};
+
+PCGB_HD constexpr int pk(int i, int j) { return i * (i + 1) / 2 + j; }  // packed lower index, j <= i
+// The reference's diagonal pivoting never picks a pivot (its max search does
+// not update the running maximum, permute.py:47-58), and its swaps (i, n-1)
+// for i = 0..n-1 (permute.py:185-192) compose to the fixed rotation
+// perm = [n-1, 0, 1, ..., n-2]. A NaN diagonal would change the swaps, but it
+// also turns every entry of the solution into NaN, which the caller zeroes.
+template <int P> PCGB_HD constexpr int rot(int i) { return i == 0 ? P - 1 : i - 1; }
+
+// GMW81 solve (solver.py:431-463) of the packed symmetric matrix A (row i,
+// column j <= i) for right-hand side b: rotate, Jacobi-scale by sqrt|diag|,
+// modified LDL^T with the reference's delta/beta rules (solver.py:23-95),
+// L D L^T solve (solver.py:298-308, 341-350), unscale, un-rotate.
+template <int P, typename T>
+PCGB_HD void gmw81_solve(const T (&A)[P * (P + 1) / 2], const T (&b)[P], T (&x)[P]) {
+  T L[P][P];
+  T r[P], s[P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    const int pi = rot<P>(i);
+    r[i] = b[pi];
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      const int pj = rot<P>(j);
+      L[i][j] = pi >= pj ? A[pk(pi, pj)] : A[pk(pj, pi)];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    s[i] = pcgb_sqrt(pcgb_abs(L[i][i]));
+    r[i] /= s[i];
+  }
+#pragma unroll
+  for (int i = 0; i < P; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) L[i][j] /= (s[i] * s[j]);
+
+  T gam = T(0), nu = T(0);
+  T beta2 = Num<T>::gmw_eps(), delta = Num<T>::gmw_eps();
+#pragma unroll
+  for (int i = 0; i < P; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      const T t = pcgb_abs(L[i][j]);
+      if (i == j) {
+        if (t > gam) gam = t;
+      } else {
+        if (t > nu) nu = t;
+      }
+    }
+  if (P > 1) nu /= pcgb_sqrt(T(P * P - 1));
+  if (beta2 < gam) beta2 = gam;
+  if (beta2 < nu) beta2 = nu;
+  if (gam + nu > T(1)) delta *= (gam + nu);
+
+#pragma unroll
+  for (int j = 0; j < P; ++j) {
+#pragma unroll
+    for (int q = 0; q < j; ++q) L[j][q] /= L[q][q];
+#pragma unroll
+    for (int i = j + 1; i < P; ++i) {
+      T t0 = L[i][j];
+#pragma unroll
+      for (int q = 0; q < j; ++q) t0 -= L[j][q] * L[i][q];
+      L[i][j] = t0;
+    }
+    T th = T(0);
+#pragma unroll
+    for (int i = j + 1; i < P; ++i) {
+      const T t = pcgb_abs(L[i][j]);
+      if (th < t) th = t;
+    }
+    th *= th;
+    T d = pcgb_abs(L[j][j]);
+    if (d < delta) d = delta;
+    const T t0 = th / beta2;
+    if (d < t0) d = t0;
+    L[j][j] = d;
+#pragma unroll
+    for (int i = j + 1; i < P; ++i) {
+      const T t = L[i][j];
+      L[i][i] -= t * t / d;
+    }
+  }
+
+  T y[P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    T t = r[i];
+#pragma unroll
+    for (int j = 0; j < i; ++j) t -= L[i][j] * L[j][j] * y[j];
+    y[i] = t / L[i][i];
+  }
+#pragma unroll
+  for (int i = P - 1; i >= 0; --i) {
+    T t = y[i];
+#pragma unroll
+    for (int j = i + 1; j < P; ++j) t -= L[j][i] * y[j];
+    y[i] = t;
+  }
+#pragma unroll
+  for (int i = 0; i < P; ++i) x[rot<P>(i)] = y[i] / s[i];
+}
+
+template <typename T> PCGB_HD T load(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
+
+// All iterations of one voxel.
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
+  constexpr int P = Model::P, H = Model::H, C = Model::C;
+  const long long N = a.N;
+  TA p[P], lo[P], hi[P], stp[P];
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    p[k] = load<TA>(a.pars, k * N + v);
+    lo[k] = SHARED_B ? Num<TA>::slb(a, k) : load<TA>(a.lb, k * a.bstride + v);
+    hi[k] = SHARED_B ? Num<TA>::sub(a, k) : load<TA>(a.ub, k * a.bstride + v);
+    stp[k] = a.step ? load<TA>(a.step, k * N + v) : TA(0);
+  }
+  TA d[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
+  TA cv[SHARED_C ? 1 : (C > 0 ? C * M : 1)];
+  if (!SHARED_C) {
+#pragma unroll
+    for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
+  }
+  TA lam = load<TA>(a.lam, v);
+  int st = a.step_type[v];
+  TA f = load<TA>(a.f, v);
+  TA first = f;
+  const TA tol = TA(a.tol), mu = TA(a.mu), eta = TA(a.eta), acc = TA(a.acc), dec = TA(a.dec);
+  int done = 0;
+
+  for (int it = 0; it < a.iters; ++it) {
+    if (st == 0) break;
+    ++done;
+    // f, g = J^T r, h = sum (J J^T + r d2m), damped diagonal (lsqnonlin.py:225-256)
+    TA fa = TA(0), g[P], h[H], hd[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) g[k] = hd[k] = TA(0);
+#pragma unroll
+    for (int k = 0; k < H; ++k) h[k] = TA(0);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      TA c[C > 0 ? C : 1];
+#pragma unroll
+      for (int k = 0; k < C; ++k) c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : cv[k * M + i];
+      TA m, J[P], Hm[H];
+      Model::template all<TA>(p, c, m, J, Hm);
+      const TA r = m - d[i];
+      fa += r * r;
+#pragma unroll
+      for (int j = 0; j < P; ++j) {
+#pragma unroll
+        for (int k = 0; k <= j; ++k) {
+          const TA jt = J[j] * J[k];
+          const TA hj = Model::hnz(pk(j, k)) ? Hm[pk(j, k)] * r + jt : jt;
+          h[pk(j, k)] += hj;
+          if (j == k) hd[j] += hj + fmax(lam * jt, Num<TA>::damp_floor());
+        }
+        g[j] += J[j] * r;
+      }
+    }
+    f = fa;
+    if (it == 0) first = f;
+
+    // damped solve in TS (lsqnonlin.py:848-878), then drop NaN/Inf (881-891)
+    {
+      TS A[H], b[P], x[P];
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        b[i] = TS(g[i]);
+#pragma unroll
+        for (int j = 0; j <= i; ++j) A[pk(i, j)] = TS(i == j ? hd[i] : h[pk(i, j)]);
+      }
+      gmw81_solve<P, TS>(A, b, x);
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        stp[k] = TA(x[k]);
+        if (!isfinite(stp[k])) stp[k] = TA(0);
+      }
+    }
+
+    // projected-gradient convergence test (lsqnonlin.py:697-723)
+    {
+      bool clamped = false;
+      TA nrm = TA(0);
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        TA t2 = p[k] - g[k];
+        if (t2 > hi[k]) {
+          clamped = true;
+          t2 = hi[k];
+        } else if (t2 < lo[k]) {
+          clamped = true;
+          t2 = lo[k];
+        }
+        t2 = p[k] - t2;
+        nrm += t2 * t2;
+      }
+      if (nrm < tol * (TA(1) + f) && ((st & 1) || clamped)) st = 0;
+      if (st == 0) break;
+    }
+
+    // trial point and its cost (lsqnonlin.py:902-912, 46-67)
+    TA pt[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) pt[k] = p[k] - stp[k];
+    TA ftp = TA(0);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      TA c[C > 0 ? C : 1];
+#pragma unroll
+      for (int k = 0; k < C; ++k) c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : cv[k * M + i];
+      const TA r = Model::template value<TA>(pt, c) - d[i];
+      ftp += r * r;
+    }
+
+    // gain ratio in TS (lsqnonlin.py:441-491)
+    {
+      const TS actual = TS(0.5) * (TS(f) - TS(ftp));
+      TS pred = TS(0);
+#pragma unroll
+      for (int i = 0; i < P; ++i)
+#pragma unroll
+        for (int j = 0; j <= i; ++j) {
+          const TS e = TS(h[pk(i, j)]) * TS(stp[i]) * TS(stp[j]);
+          pred -= (i == j) ? e : TS(2) * e;
+        }
+      pred *= TS(0.5);
+#pragma unroll
+      for (int i = 0; i < P; ++i) pred += TS(stp[i]) * TS(g[i]);
+      const TS rho = actual / pred;
+      if ((rho > TS(mu)) && (actual > TS(0))) {
+#pragma unroll
+        for (int k = 0; k < P; ++k) p[k] = pt[k];
+        if (rho > TS(eta)) {
+          lam *= acc;
+          st = 1;
+        } else {
+          st = 2;
+        }
+      } else {
+        lam *= dec;
+        st = 4;
+      }
+      if (pred < TS(0)) {
+        lam *= dec;
+        st |= 8;
+      }
+    }
+    // box projection (lsqnonlin.py:590-601)
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      if (p[k] > hi[k])
+        p[k] = hi[k];
+      else if (p[k] < lo[k])
+        p[k] = lo[k];
+    }
+  }
+
+  TA* pars = static_cast<TA*>(a.pars);
+#pragma unroll
+  for (int k = 0; k < P; ++k) pars[k * N + v] = p[k];
+  if (a.step) {
+#pragma unroll
+    for (int k = 0; k < P; ++k) static_cast<TA*>(a.step)[k * N + v] = stp[k];
+  }
+  static_cast<TA*>(a.lam)[v] = lam;
+  a.step_type[v] = static_cast<signed char>(st);
+  static_cast<TA*>(a.f)[v] = f;
+  if (a.iters > 0) {
+    static_cast<TA*>(a.first_f)[v] = first;
+    static_cast<TA*>(a.last_f)[v] = f;
+  }
+  if (a.iters_done) a.iters_done[v] += done;
+}
+
+// Grid-stride schedule: thread t fits voxels t, t + T, t + 2T, ...
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+__device__ void lm_grid(const PcgbLmParams& a) {
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.N; v += T)
+    lm_fit_voxel<Model, M, TA, TS, SHARED_C, SHARED_B>(a, v);
+}
+
+// Accumulating cost, the reference F kernel (lsqnonlin.py:157-177, 46-67):
+// f[v] += sum_i (m(p_v; c_i) - d_i)^2, voxels with step_type == 0 skipped.
+template <class Model, int M, typename TA, bool SHARED_C>
+__device__ void cost_grid(const PcgbLmParams& a) {
+  constexpr int P = Model::P, C = Model::C;
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.N; v += T) {
+    if (a.step_type && a.step_type[v] == 0) continue;
+    TA p[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * a.N + v);
+    TA fa = TA(0);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      TA c[C > 0 ? C : 1];
+#pragma unroll
+      for (int k = 0; k < C; ++k)
+        c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : load<TA>(a.consts, (k * M + i) * a.cstride + v);
+      const TA r = Model::template value<TA>(p, c) - load<TA>(a.data, i * a.N + v);
+      fa += r * r;
+    }
+    static_cast<TA*>(a.f)[v] += fa;
+  }
+}
+
+// Batched GMW81 solve (the reference GMW81Solver kernel, solver.py:526-563):
+// consts holds the packed (H, N) matrices, data the (P, N) right-hand sides,
+// step receives the (P, N) solutions.
+template <int P, typename T>
+__device__ void gmw81_grid(const PcgbLmParams& a) {
+  constexpr int H = P * (P + 1) / 2;
+  const long long T_ = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.N; v += T_) {
+    T A[H], b[P], x[P];
+#pragma unroll
+    for (int q = 0; q < H; ++q) A[q] = load<T>(a.consts, q * a.N + v);
+#pragma unroll
+    for (int k = 0; k < P; ++k) b[k] = load<T>(a.data, k * a.N + v);
+    gmw81_solve<P, T>(A, b, x);
+#pragma unroll
+    for (int k = 0; k < P; ++k) static_cast<T*>(a.step)[k * a.N + v] = x[k];
+  }
+}
+
+}  // namespace pcgb

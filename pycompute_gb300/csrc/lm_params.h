@@ -1,0 +1,39 @@
+// Launch parameters of the LM kernels. Shared by the host library (pcgb.cpp)
+// and the kernel source that is compiled at run time, so it must stay plain C
+// with fixed-size members.
+#pragma once
+
+#define PCGB_MAX_PARAMS 8
+#define PCGB_MAX_PROTOCOL 256
+
+struct PcgbLmParams {
+  // structure-of-arrays, voxel index fastest; element type is the fitter's
+  // state type (float, or double for the all-FP64 build)
+  void* pars;              // (P, N) in/out
+  const void* consts;      // (C*M, N) per voxel, unused when the protocol is shared
+  const void* data;        // (M, N)
+  const void* lb;          // (P, N) per voxel, unused when bounds are shared
+  const void* ub;          // (P, N)
+  void* lam;               // (N) in/out damping
+  signed char* step_type;  // (N) in/out, 0 = converged
+  void* f;                 // (N) in/out cost at the last evaluated iterate
+  void* first_f;           // (N) out, cost after the first iteration of the call
+  void* last_f;            // (N) out, cost after the last iteration of the call
+  void* step;              // (P, N) out or null
+  int* iters_done;         // (N) in/out iteration counter or null
+  unsigned int* work;      // voxel work counter of the persistent schedule (zeroed by the host) or null
+  long long N;
+  long long cstride;       // N: per-voxel constants; 0: protocol_* hold them
+  long long bstride;       // N: per-voxel bounds; 0: shared_* hold them
+  int iters;
+  int flags;
+  double tol, mu, eta, acc, dec;
+  // shared protocol and bounds in both precisions, so the kernel reads its own
+  // type straight from the parameter bank (constant k of sample i at k*M + i)
+  float shared_lb_f[PCGB_MAX_PARAMS];
+  float shared_ub_f[PCGB_MAX_PARAMS];
+  double shared_lb_d[PCGB_MAX_PARAMS];
+  double shared_ub_d[PCGB_MAX_PARAMS];
+  float protocol_f[PCGB_MAX_PROTOCOL];
+  double protocol_d[PCGB_MAX_PROTOCOL];
+};

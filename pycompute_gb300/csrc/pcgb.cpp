@@ -1,0 +1,403 @@
+// Host side of the C ABI in include/pcgb.h.
+//
+// A fitter is one NVRTC-compiled program: the embedded device sources
+// (lm_params.h, lm_kernel.cuh) plus the caller's generated model struct, with
+// the LM, cost and GMW81 kernels instantiated for the model's P, C and M and
+// the chosen precision. Programs are compiled for sm_103a to a cubin, cached
+// on disk by a hash of the full source and options, and loaded with
+// cudaLibraryLoadData. Only the CUDA runtime is used (cudart is linked
+// statically and opens the driver on first use), so the library also loads on
+// a host without a GPU.
+#include "pcgb.h"
+
+#include <cuda_runtime.h>
+#include <nvrtc.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "lm_params.h"
+
+extern const char* pcgb_embedded_lm_params_h;
+extern const char* pcgb_embedded_lm_kernel_cuh;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[2048];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(PCGB_ECUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
+  for (unsigned char c : s) {
+    h ^= c;
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+enum KernelSlot { K_LM_C1_B1, K_LM_C1_B0, K_LM_C0_B1, K_LM_C0_B0, K_COST_C1, K_COST_C0, K_GMW, K_COUNT };
+const char* kKernelNames[K_COUNT] = {"pcgb_lm_c1_b1", "pcgb_lm_c1_b0", "pcgb_lm_c0_b1", "pcgb_lm_c0_b0",
+                                     "pcgb_cost_c1",  "pcgb_cost_c0",  "pcgb_gmw81"};
+
+constexpr int kDefaultBlock = 128;
+constexpr int kMaxBlock = 256;
+
+}  // namespace
+
+struct pcgb_fitter {
+  int P = 0, C = 0, M = 0, dtype = 0, sdtype = 0;
+  int device = -1;
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t k[K_COUNT] = {};
+  std::string log;
+};
+
+namespace {
+
+std::string program_source(const char* model_source, const char* model_struct, int P, int C, int M, int dtype,
+                           int sdtype) {
+  const char* ta = dtype == PCGB_DTYPE_F64 ? "double" : "float";
+  const char* ts = sdtype == PCGB_DTYPE_F64 ? "double" : "float";
+  std::ostringstream s;
+  s << "// pcgb fitter program: P=" << P << " C=" << C << " M=" << M << " state=" << ta << " solve=" << ts << "\n";
+  s << pcgb_embedded_lm_params_h << "\n" << pcgb_embedded_lm_kernel_cuh << "\n" << model_source << "\n";
+  s << "typedef " << model_struct << " PcgbModel;\n";
+  s << "static_assert(PcgbModel::P == " << P << " && PcgbModel::C == " << C << ", \"model shape\");\n";
+  const char* bounds = "__launch_bounds__(256)";
+  for (int c = 1; c >= 0; --c)
+    for (int b = 1; b >= 0; --b)
+      s << "extern \"C\" __global__ void " << bounds << " pcgb_lm_c" << c << "_b" << b
+        << "(const PcgbLmParams a) { pcgb::lm_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
+        << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
+  for (int c = 1; c >= 0; --c)
+    s << "extern \"C\" __global__ void " << bounds << " pcgb_cost_c" << c
+      << "(const PcgbLmParams a) { pcgb::cost_grid<PcgbModel, " << M << ", " << ta << ", " << (c ? "true" : "false")
+      << ">(a); }\n";
+  s << "extern \"C\" __global__ void " << bounds << " pcgb_gmw81(const PcgbLmParams a) { pcgb::gmw81_grid<" << P
+    << ", " << ts << ">(a); }\n";
+  return s.str();
+}
+
+const std::vector<std::string>& nvrtc_options() {
+  static const std::vector<std::string> opts = {"--gpu-architecture=sm_103a", "-std=c++17", "-lineinfo",
+                                                "--ptxas-options=-v", "-default-device"};
+  return opts;
+}
+
+int compile_cubin(const std::string& src, std::vector<char>& cubin, std::string& log) {
+  nvrtcProgram prog;
+  nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "pcgb_fitter.cu", 0, nullptr, nullptr);
+  if (r != NVRTC_SUCCESS) return fail(PCGB_ECOMPILE, "nvrtcCreateProgram: %s", nvrtcGetErrorString(r));
+  std::vector<const char*> o;
+  for (auto& s : nvrtc_options()) o.push_back(s.c_str());
+  r = nvrtcCompileProgram(prog, int(o.size()), o.data());
+  size_t ls = 0;
+  nvrtcGetProgramLogSize(prog, &ls);
+  log.assign(ls, '\0');
+  if (ls) nvrtcGetProgramLog(prog, &log[0]);
+  while (!log.empty() && log.back() == '\0') log.pop_back();
+  if (r != NVRTC_SUCCESS) {
+    nvrtcDestroyProgram(&prog);
+    return fail(PCGB_ECOMPILE, "NVRTC compile failed (%s):\n%s", nvrtcGetErrorString(r), log.c_str());
+  }
+  size_t n = 0;
+  r = nvrtcGetCUBINSize(prog, &n);
+  if (r != NVRTC_SUCCESS || n == 0) {
+    nvrtcDestroyProgram(&prog);
+    return fail(PCGB_ECOMPILE, "nvrtcGetCUBINSize: %s", nvrtcGetErrorString(r));
+  }
+  cubin.resize(n);
+  r = nvrtcGetCUBIN(prog, cubin.data());
+  nvrtcDestroyProgram(&prog);
+  if (r != NVRTC_SUCCESS) return fail(PCGB_ECOMPILE, "nvrtcGetCUBIN: %s", nvrtcGetErrorString(r));
+  return PCGB_OK;
+}
+
+bool read_file(const std::string& path, std::vector<char>& out) {
+  std::ifstream f(path, std::ios::binary);
+  if (!f) return false;
+  out.assign(std::istreambuf_iterator<char>(f), std::istreambuf_iterator<char>());
+  return !out.empty();
+}
+
+void write_file_atomic(const std::string& path, const std::vector<char>& data) {
+  std::string tmp = path + ".tmp" + std::to_string(reinterpret_cast<uintptr_t>(&data));
+  {
+    std::ofstream f(tmp, std::ios::binary);
+    if (!f) return;
+    f.write(data.data(), std::streamsize(data.size()));
+    if (!f) return;
+  }
+  std::rename(tmp.c_str(), path.c_str());
+}
+
+int check_device(const pcgb_fitter* ft) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (ft->device >= 0 && dev != ft->device)
+    return fail(PCGB_EINVAL, "fitter was built on device %d but device %d is current", ft->device, dev);
+  return PCGB_OK;
+}
+
+int grid_for(int64_t n, int block) {
+  int64_t g = (n + block - 1) / block;
+  if (g < 1) g = 1;
+  if (g > (int64_t(1) << 30)) g = int64_t(1) << 30;
+  return int(g);
+}
+
+int launch(pcgb_fitter* ft, KernelSlot slot, const PcgbLmParams& prm, int64_t n, int block, void* stream) {
+  if (!ft->k[slot]) return fail(PCGB_EINVAL, "kernel %s missing from program", kKernelNames[slot]);
+  if (block <= 0) block = kDefaultBlock;
+  if (block > kMaxBlock || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to %d", kMaxBlock);
+  if (n == 0) return PCGB_OK;
+  PcgbLmParams local = prm;
+  void* args[] = {&local};
+  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(ft->k[slot]), dim3(grid_for(n, block)),
+                                   dim3(block), args, 0, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, kKernelNames[slot]);
+  return PCGB_OK;
+}
+
+int fill_protocol(const pcgb_fitter* ft, PcgbLmParams& prm, int64_t cstride, int64_t n, const double* protocol,
+                  int protocol_len) {
+  if (cstride == 0) {
+    const int need = ft->C * ft->M;
+    if (need > PCGB_MAX_PROTOCOL) return fail(PCGB_ERANGE, "protocol of %d values exceeds %d", need, PCGB_MAX_PROTOCOL);
+    if (need > 0 && (!protocol || protocol_len != need))
+      return fail(PCGB_EINVAL, "shared protocol needs %d host values, got %d", need, protocol ? protocol_len : 0);
+    for (int i = 0; i < need; ++i) {
+      prm.protocol_d[i] = protocol[i];
+      prm.protocol_f[i] = float(protocol[i]);
+    }
+  } else if (cstride != n) {
+    return fail(PCGB_EINVAL, "consts_stride must be 0 (shared protocol) or nprobs");
+  }
+  prm.cstride = cstride;
+  return PCGB_OK;
+}
+
+}  // namespace
+
+namespace {
+
+int validate_create(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata, int dtype,
+                    int solve_dtype) {
+  if (!model_source || !model_struct || !*model_struct) return fail(PCGB_EINVAL, "model source/struct missing");
+  if (nparam < 1 || nparam > PCGB_MAX_PARAMS) return fail(PCGB_ERANGE, "nparam %d outside 1..%d", nparam, PCGB_MAX_PARAMS);
+  if (nconst < 0 || ndata < 1 || int64_t(nconst) * ndata > PCGB_MAX_PROTOCOL)
+    return fail(PCGB_ERANGE, "nconst*ndata must fit %d (nconst=%d, ndata=%d)", PCGB_MAX_PROTOCOL, nconst, ndata);
+  if ((dtype != PCGB_DTYPE_F32 && dtype != PCGB_DTYPE_F64) ||
+      (solve_dtype != PCGB_DTYPE_F32 && solve_dtype != PCGB_DTYPE_F64))
+    return fail(PCGB_EINVAL, "dtype must be 0 (float32) or 1 (float64)");
+  if (dtype == PCGB_DTYPE_F64 && solve_dtype == PCGB_DTYPE_F32)
+    return fail(PCGB_EINVAL, "a float64 state with a float32 solve is not supported");
+  return PCGB_OK;
+}
+
+// Compiled cubin of the program, from the disk cache when present.
+int get_cubin(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata, int dtype,
+              int solve_dtype, const char* cache_dir, std::vector<char>& cubin, std::string& log) {
+  const std::string src = program_source(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype);
+  std::string key_src = src;
+  for (auto& o : nvrtc_options()) key_src += "\n" + o;
+  int nv_major = 0, nv_minor = 0;
+  nvrtcVersion(&nv_major, &nv_minor);
+  key_src += "\nnvrtc " + std::to_string(nv_major) + "." + std::to_string(nv_minor);
+  char keyhex[32];
+  std::snprintf(keyhex, sizeof(keyhex), "%016llx", (unsigned long long)fnv1a(key_src));
+  std::string cache_path;
+  if (cache_dir && *cache_dir) cache_path = std::string(cache_dir) + "/pcgb_" + keyhex + ".cubin";
+  if (cache_path.empty() || !read_file(cache_path, cubin)) {
+    int rc = compile_cubin(src, cubin, log);
+    if (rc) return rc;
+    if (!cache_path.empty()) write_file_atomic(cache_path, cubin);
+  }
+  return PCGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* pcgb_version(void) { return "pycompute-gb300 0.1 (sm_103a)"; }
+int pcgb_max_params(void) { return PCGB_MAX_PARAMS; }
+int pcgb_max_protocol(void) { return PCGB_MAX_PROTOCOL; }
+const char* pcgb_last_error(void) { return g_err.c_str(); }
+
+int pcgb_fitter_compile(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata,
+                        int dtype, int solve_dtype, const char* cache_dir, char* log_buf, size_t log_len) {
+  g_err.clear();
+  if (int rc = validate_create(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype)) return rc;
+  std::vector<char> cubin;
+  std::string log;
+  if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, cubin, log))
+    return rc;
+  if (log_buf && log_len) {
+    std::snprintf(log_buf, log_len, "%s", log.c_str());
+  }
+  return PCGB_OK;
+}
+
+int pcgb_fitter_create(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata,
+                       int dtype, int solve_dtype, const char* cache_dir, pcgb_fitter** out) {
+  g_err.clear();
+  if (!out) return fail(PCGB_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (int rc = validate_create(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype)) return rc;
+  std::vector<char> cubin;
+  std::string log;
+  if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, cubin, log))
+    return rc;
+
+  auto* ft = new (std::nothrow) pcgb_fitter();
+  if (!ft) return fail(PCGB_ENOMEM, "out of host memory");
+  ft->P = nparam;
+  ft->C = nconst;
+  ft->M = ndata;
+  ft->dtype = dtype;
+  ft->sdtype = solve_dtype;
+  ft->log = log;
+  cudaError_t e = cudaGetDevice(&ft->device);
+  if (e != cudaSuccess) {
+    delete ft;
+    return cuda_fail(e, "cudaGetDevice");
+  }
+  e = cudaLibraryLoadData(&ft->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) {
+    delete ft;
+    return cuda_fail(e, "cudaLibraryLoadData");
+  }
+  for (int i = 0; i < K_COUNT; ++i) {
+    e = cudaLibraryGetKernel(&ft->k[i], ft->lib, kKernelNames[i]);
+    if (e != cudaSuccess) {
+      cudaLibraryUnload(ft->lib);
+      delete ft;
+      return cuda_fail(e, kKernelNames[i]);
+    }
+  }
+  *out = ft;
+  return PCGB_OK;
+}
+
+int pcgb_fitter_destroy(pcgb_fitter* ft) {
+  if (!ft) return PCGB_OK;
+  int rc = PCGB_OK;
+  if (ft->lib) {
+    cudaError_t e = cudaLibraryUnload(ft->lib);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaLibraryUnload");
+  }
+  delete ft;
+  return rc;
+}
+
+const char* pcgb_fitter_log(const pcgb_fitter* ft) { return ft ? ft->log.c_str() : ""; }
+
+int pcgb_lm_run(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type, void* f,
+                void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host, int block,
+                void* stream) {
+  g_err.clear();
+  if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
+  if (nprobs < 0 || iters < 0) return fail(PCGB_EINVAL, "nprobs and iters must be >= 0");
+  if (nprobs > 0 && (!data || !params || !lam || !step_type || !f || !first_f || !last_f))
+    return fail(PCGB_EINVAL, "data, params, lam, step_type, f, first_f and last_f are required");
+  if (int rc = check_device(ft)) return rc;
+  PcgbLmParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  if (int rc = fill_protocol(ft, prm, consts_stride, nprobs, protocol_host, protocol_len)) return rc;
+  if (consts_stride != 0 && !consts) return fail(PCGB_EINVAL, "per-voxel consts pointer is NULL");
+  if (bounds_stride == 0) {
+    if (!lb_host || !ub_host) return fail(PCGB_EINVAL, "shared bounds need lb_host and ub_host");
+    for (int k = 0; k < ft->P; ++k) {
+      prm.shared_lb_d[k] = lb_host[k];
+      prm.shared_ub_d[k] = ub_host[k];
+      prm.shared_lb_f[k] = float(lb_host[k]);
+      prm.shared_ub_f[k] = float(ub_host[k]);
+    }
+  } else if (bounds_stride != nprobs || !lower_bound || !upper_bound) {
+    return fail(PCGB_EINVAL, "bounds_stride must be 0 (shared) or nprobs with device bounds");
+  }
+  prm.pars = params;
+  prm.consts = consts;
+  prm.data = data;
+  prm.lb = lower_bound;
+  prm.ub = upper_bound;
+  prm.lam = lam;
+  prm.step_type = reinterpret_cast<signed char*>(step_type);
+  prm.f = f;
+  prm.first_f = first_f;
+  prm.last_f = last_f;
+  prm.step = step;
+  prm.iters_done = iters_done;
+  prm.N = nprobs;
+  prm.bstride = bounds_stride;
+  prm.iters = iters;
+  prm.tol = tol;
+  prm.mu = mu;
+  prm.eta = eta;
+  prm.acc = acc;
+  prm.dec = dec;
+  const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_LM_C1_B1 : K_LM_C1_B0)
+                                             : (bounds_stride == 0 ? K_LM_C0_B1 : K_LM_C0_B0);
+  return launch(ft, slot, prm, nprobs, block, stream);
+}
+
+int pcgb_f_run(pcgb_fitter* ft, const void* params, const void* consts, int64_t consts_stride, const void* data,
+               const int8_t* step_type, void* f, int64_t nprobs, const double* protocol_host, int protocol_len,
+               void* stream) {
+  g_err.clear();
+  if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
+  if (nprobs < 0) return fail(PCGB_EINVAL, "nprobs must be >= 0");
+  if (nprobs > 0 && (!params || !data || !f)) return fail(PCGB_EINVAL, "params, data and f are required");
+  if (int rc = check_device(ft)) return rc;
+  PcgbLmParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  if (int rc = fill_protocol(ft, prm, consts_stride, nprobs, protocol_host, protocol_len)) return rc;
+  if (consts_stride != 0 && !consts) return fail(PCGB_EINVAL, "per-voxel consts pointer is NULL");
+  prm.pars = const_cast<void*>(params);
+  prm.consts = consts;
+  prm.data = data;
+  prm.step_type = const_cast<signed char*>(reinterpret_cast<const signed char*>(step_type));
+  prm.f = f;
+  prm.N = nprobs;
+  return launch(ft, consts_stride == 0 ? K_COST_C1 : K_COST_C0, prm, nprobs, 0, stream);
+}
+
+int pcgb_gmw81_solve(pcgb_fitter* ft, const void* mat, const void* rhs, void* sol, int64_t nprobs, void* stream) {
+  g_err.clear();
+  if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
+  if (nprobs < 0) return fail(PCGB_EINVAL, "nprobs must be >= 0");
+  if (nprobs > 0 && (!mat || !rhs || !sol)) return fail(PCGB_EINVAL, "mat, rhs and sol are required");
+  if (int rc = check_device(ft)) return rc;
+  PcgbLmParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  prm.consts = mat;
+  prm.data = rhs;
+  prm.step = sol;
+  prm.N = nprobs;
+  return launch(ft, K_GMW, prm, nprobs, 0, stream);
+}
+
+}  // extern "C"

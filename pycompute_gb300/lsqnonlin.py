@@ -1,0 +1,377 @@
+"""Drop-in fitter classes with the reference's call surface.
+
+Mirrors ``pycompute/cuda/lsqnonlin.py``: ``Expr``, ``F_GradF``, ``F``,
+``SecondOrderLevenbergMarquardt`` (and ``GMW81Solver`` from
+``pycompute/cuda/solver.py``), with the same constructor arguments, the same
+``setup``/``run`` split, the same array layouts and the same result attributes
+(``pars_t`` updated in place, ``f_t``, ``first_f``, ``last_f``,
+``step_type_t``, ``lam_t``, ``step_t``).
+
+Arrays are PyTorch CUDA tensors (CuPy arrays and anything else exporting
+DLPack are accepted and viewed as tensors without a copy). PyTorch is used for
+buffers and the current stream only; all fitting runs in libpcgb.so.
+
+Differences from the reference, all deliberate:
+* one launch runs every iteration of ``run`` (the reference launches once per
+  iteration); results are the same per voxel;
+* the GMW81 solve and gain-ratio test run in float64 for float32 fitters
+  (``solve_dtype``); pass ``solve_dtype=torch.float32`` for the reference's
+  all-fp32 arithmetic;
+* a protocol shared by every voxel may be passed as a (C*M,) or (C*M, 1)
+  tensor and bounds as (P,) or (P, 1); it is then held in the kernel's
+  parameter bank instead of being read per voxel. A (C*M, N) consts tensor
+  whose columns are all equal is detected and treated the same way;
+* ``run`` validates its inputs and raises instead of reading out of bounds.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Optional
+
+import torch
+
+from . import _lib, codegen
+
+_TORCH_DTYPES = {torch.float32: 0, torch.float64: 1}
+
+
+def _as_tensor(x, name: str) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        return x
+    if hasattr(x, "__dlpack__"):
+        return torch.from_dlpack(x)
+    raise TypeError(f"{name} must be a torch tensor or a DLPack-capable array, got {type(x)}")
+
+
+def _dtype(d) -> torch.dtype:
+    if isinstance(d, torch.dtype):
+        return d
+    s = getattr(d, "name", None) or getattr(d, "__name__", None) or str(d)
+    s = str(s).replace("numpy.", "").replace("cupy.", "")
+    if s in ("float32", "f", "float"):
+        return torch.float32
+    if s in ("float64", "d", "double"):
+        return torch.float64
+    raise RuntimeError(f"does only support fp32 and fp64, got {d}")
+
+
+def _stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def _ptr(t: Optional[torch.Tensor]):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+class Expr:
+    """Model specification (reference ``Expr``, lsqnonlin.py:21-28)."""
+
+    def __init__(self, expr: str, pars_str: list[str], consts_str: list[str],
+                 nonlin_terms: list[str] | None = None, nonlin_pars: list[int] | None = None):
+        self.expr = expr
+        self.pars_str = list(pars_str)
+        self.consts_str = list(consts_str)
+        self.nonlin_terms = nonlin_terms
+        self.nonlin_pars = nonlin_pars
+
+
+class F_GradF:
+    """User-supplied model code (reference ``F_GradF``, lsqnonlin.py:32-39).
+
+    In the reference ``f`` and ``gradf`` are CudaFunction objects whose device
+    code computes the cost and the accumulated derivatives. Here the user
+    supplies one model struct in the generated form (see ``codegen``):
+    ``source`` defines ``struct <name>`` with ``P``, ``C``, ``H``, ``jnz``,
+    ``hnz``, ``value`` and ``all``.
+    """
+
+    def __init__(self, source: str, nparam: int, nconst: int, name: str):
+        self.source = source
+        self.nparam = nparam
+        self.nconst = nconst
+        self.name = name
+
+
+def _funcid(prefix: str, P: int, C: int, M: int, dtype: torch.dtype, tag: str) -> str:
+    t = "f" if dtype == torch.float32 else "d"
+    return f"{prefix}_{P}_{C}_{M}_{t}_{tag}"
+
+
+class _Program:
+    """One compiled fitter program (model x protocol length x precision)."""
+
+    _cache: dict = {}
+
+    def __init__(self, source: str, struct: str, P: int, C: int, M: int, dtype: torch.dtype,
+                 solve_dtype: torch.dtype):
+        L = _lib.lib()
+        h = ctypes.c_void_p()
+        dev = torch.cuda.current_device()
+        rc = L.pcgb_fitter_create(source.encode(), struct.encode(), P, C, M, _TORCH_DTYPES[dtype],
+                                  _TORCH_DTYPES[solve_dtype], _lib.cache_dir().encode(), ctypes.byref(h))
+        _lib.check("pcgb_fitter_create", rc)
+        self.handle = h
+        self.device = dev
+        self.P, self.C, self.M, self.dtype, self.solve_dtype = P, C, M, dtype, solve_dtype
+        self.log = L.pcgb_fitter_log(h).decode(errors="replace")
+
+    @classmethod
+    def get(cls, source, struct, P, C, M, dtype, solve_dtype):
+        key = (source, struct, P, C, M, dtype, solve_dtype, torch.cuda.current_device())
+        prog = cls._cache.get(key)
+        if prog is None:
+            prog = cls(source, struct, P, C, M, dtype, solve_dtype)
+            cls._cache[key] = prog
+        return prog
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                _lib.lib().pcgb_fitter_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def _model_from(model_expr, f_gradf, legacy) -> tuple[str, str, int, int, str, Optional[Expr]]:
+    if legacy is not None:
+        expr, pars_str, consts_str = legacy
+        model_expr = Expr(expr, pars_str, consts_str)
+    if model_expr is not None and f_gradf is None:
+        gm = codegen.generate(model_expr.expr, model_expr.pars_str, model_expr.consts_str)
+        return gm.source, gm.struct_name, gm.P, gm.C, gm.hash, model_expr
+    if f_gradf is not None and model_expr is None:
+        return f_gradf.source, f_gradf.name, f_gradf.nparam, f_gradf.nconst, f_gradf.name, None
+    raise RuntimeError("One and only one of model_expr or f_gradf must be non None")
+
+
+def _shared_rows(t: torch.Tensor, rows: int, n: int, name: str, detect: bool):
+    """Classify a (rows, N) / (rows, 1) / (rows,) tensor: (tensor, stride, host values)."""
+    if t.dim() == 1:
+        t = t.reshape(rows, 1)
+    if t.dim() != 2 or t.shape[0] != rows:
+        raise RuntimeError(f"{name} must have {rows} rows, got shape {tuple(t.shape)}")
+    if t.shape[1] == 1 and n != 1:
+        return t, 0, t[:, 0].double().cpu().tolist()
+    if t.shape[1] != n:
+        raise RuntimeError(f"{name} must have 1 or {n} columns, got {t.shape[1]}")
+    if detect and n > 0 and bool((t == t[:, :1]).all()):
+        return t, 0, t[:, 0].double().cpu().tolist()
+    return t, n, None
+
+
+def _parse_ctor(args, kwargs, names):
+    """Constructor arguments in the reference's two call forms.
+
+    Expression form (lsqnonlin.py:950): ``(model_expr: Expr | None, [f_gradf,] ndata, dtype, write_to_file)``.
+    Notebook form (test_ivim.ipynb cell 16): ``(expr: str, pars_str, consts_str, ndata=, dtype=, write_to_file=)``.
+    Returns (model_expr, f_gradf, legacy, ndata, dtype, write_to_file).
+    """
+    args = list(args)
+    kw = dict(kwargs)
+    legacy = None
+    if (args and isinstance(args[0], str)) or isinstance(kw.get("expr"), str):
+        expr = args.pop(0) if args else kw.pop("expr")
+        pars_str = args.pop(0) if args else kw.pop("pars_str")
+        consts_str = args.pop(0) if args else kw.pop("consts_str")
+        legacy = (expr, list(pars_str), list(consts_str))
+        rest = [n for n in names if n not in ("model_expr", "f_gradf")]
+        vals = {"model_expr": None, "f_gradf": None}
+    else:
+        rest = list(names)
+        vals = {}
+    for n in rest:
+        if args:
+            vals[n] = args.pop(0)
+        elif n in kw:
+            vals[n] = kw.pop(n)
+    if args or kw:
+        raise TypeError(f"unexpected constructor arguments: {args} {sorted(kw)}")
+    return (vals.get("model_expr"), vals.get("f_gradf"), legacy, vals.get("ndata"),
+            vals.get("dtype", torch.float32), vals.get("write_to_file", False))
+
+
+class SecondOrderLevenbergMarquardt:
+    """Batched second-order LM with GMW81 damped solves, one voxel per thread.
+
+    Same surface as the reference class (lsqnonlin.py:949-1073)::
+
+        solm = SecondOrderLevenbergMarquardt(Expr(expr, pars, consts), None, ndata, torch.float32)
+        solm = SecondOrderLevenbergMarquardt(expr, pars, consts, ndata=21, dtype=torch.float32)  # notebook form
+        solm.setup(pars_t, consts_t, data_t, lower_bound_t, upper_bound_t)
+        solm.run(50, 1e-10)
+        solm.pars_t, solm.first_f, solm.last_f, solm.step_type_t
+    """
+
+    def __init__(self, *args, solve_dtype=None, detect_shared: bool = True, **kwargs):
+        model_expr, f_gradf, legacy, ndata, dtype, write_to_file = _parse_ctor(
+            args, kwargs, ("model_expr", "f_gradf", "ndata", "dtype", "write_to_file"))
+        if ndata is None or int(ndata) < 1:
+            raise RuntimeError("ndata must be a positive integer")
+        self.dtype = _dtype(dtype)
+        self.solve_dtype = _dtype(solve_dtype) if solve_dtype is not None else torch.float64
+        if self.dtype == torch.float64 and self.solve_dtype == torch.float32:
+            raise RuntimeError("a float64 fitter solves in float64")
+        src, struct, P, C, tag, mexpr = _model_from(model_expr, f_gradf, legacy)
+        self.model_expr = mexpr
+        self.expr = mexpr.expr if mexpr else None
+        self.pars_str = list(mexpr.pars_str) if mexpr else None
+        self.consts_str = list(mexpr.consts_str) if mexpr else None
+        self.nparam, self.nconst, self.ndata = P, C, int(ndata)
+        self.nhes = P * (P + 1) // 2
+        self.write_to_file = write_to_file
+        self.detect_shared = detect_shared
+        self.funcid = _funcid("second_order_levenberg_marquardt", P, C, self.ndata, self.dtype, tag)
+        self._source, self._struct = src, struct
+        if write_to_file:
+            with open(self.funcid + ".cu", "w") as f:
+                f.write(src)
+        self._prog = None
+        self.Nprobs = 1
+
+    def build(self):
+        """Compile (NVRTC, sm_103a) and load the program on the current device."""
+        if self._prog is None or self._prog.device != torch.cuda.current_device():
+            self._prog = _Program.get(self._source, self._struct, self.nparam, self.nconst, self.ndata,
+                                      self.dtype, self.solve_dtype)
+        return self._prog
+
+    def get_device_funcid(self):
+        return self.funcid
+
+    def get_kernel_funcid(self):
+        return "k_" + self.funcid
+
+    def setup(self, pars_t, consts_t, data_t, lower_bound_t, upper_bound_t):
+        """Bind caller-owned arrays and allocate the fitter state (lsqnonlin.py:1036-1056)."""
+        pars_t = _as_tensor(pars_t, "pars_t")
+        data_t = _as_tensor(data_t, "data_t")
+        consts_t = _as_tensor(consts_t, "consts_t")
+        lower_bound_t = _as_tensor(lower_bound_t, "lower_bound_t")
+        upper_bound_t = _as_tensor(upper_bound_t, "upper_bound_t")
+        P, M, C = self.nparam, self.ndata, self.nconst
+        if data_t.dim() != 2 or data_t.shape[0] != M:
+            raise RuntimeError(f"data_t must be ({M}, N), got {tuple(data_t.shape)}")
+        N = int(data_t.shape[1])
+        for name, t in (("pars_t", pars_t), ("data_t", data_t), ("consts_t", consts_t),
+                        ("lower_bound_t", lower_bound_t), ("upper_bound_t", upper_bound_t)):
+            if not t.is_cuda:
+                raise RuntimeError(f"{name} must be a CUDA tensor")
+            if t.dtype != self.dtype:
+                raise RuntimeError(f"{name} must be {self.dtype}, got {t.dtype}")
+            if not t.is_contiguous():
+                raise RuntimeError(f"{name} must be C-contiguous")
+        if tuple(pars_t.shape) != (P, N):
+            raise RuntimeError(f"pars_t must be ({P}, {N}), got {tuple(pars_t.shape)}")
+        self.Nprobs = N
+        self.pars_t = pars_t
+        self.data_t = data_t
+        self.consts_t, self._cstride, self._protocol = _shared_rows(consts_t, C * M, N, "consts_t",
+                                                                      self.detect_shared)
+        self.lower_bound_t, bs_l, lbv = _shared_rows(lower_bound_t, P, N, "lower_bound_t", self.detect_shared)
+        self.upper_bound_t, bs_u, ubv = _shared_rows(upper_bound_t, P, N, "upper_bound_t", self.detect_shared)
+        if bs_l != bs_u:
+            if bs_l == 0:
+                self.lower_bound_t, bs_l, lbv = _shared_rows(lower_bound_t.expand(P, N).contiguous(), P, N, "lb", False)
+            if bs_u == 0:
+                self.upper_bound_t, bs_u, ubv = _shared_rows(upper_bound_t.expand(P, N).contiguous(), P, N, "ub", False)
+        self._bstride = bs_l
+        self._lb_host, self._ub_host = lbv, ubv
+        dev = pars_t.device
+        self.first_f = torch.empty((1, N), dtype=self.dtype, device=dev)
+        self.last_f = torch.empty((1, N), dtype=self.dtype, device=dev)
+        self.lam_t = torch.full((1, N), 5.0, dtype=self.dtype, device=dev)
+        self.step_t = torch.zeros((P, N), dtype=self.dtype, device=dev)
+        self.f_t = torch.zeros((1, N), dtype=self.dtype, device=dev)
+        self.step_type_t = torch.ones((1, N), dtype=torch.int8, device=dev)
+        self.iters_t = torch.zeros((1, N), dtype=torch.int32, device=dev)
+        with torch.cuda.device(dev):
+            self.build()
+
+    def run(self, iters: int, tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0, block: int = 0):
+        """Run ``iters`` iterations on every voxel (lsqnonlin.py:1058-1073). Asynchronous; returns None."""
+        if not hasattr(self, "pars_t"):
+            raise RuntimeError("setup() must be called before run()")
+        with torch.cuda.device(self.pars_t.device):
+            prog = self.build()
+            L = _lib.lib()
+            proto = (ctypes.c_double * max(1, len(self._protocol or [])))(*(self._protocol or [0.0]))
+            lbh = (ctypes.c_double * self.nparam)(*(self._lb_host or [0.0] * self.nparam))
+            ubh = (ctypes.c_double * self.nparam)(*(self._ub_host or [0.0] * self.nparam))
+            rc = L.pcgb_lm_run(prog.handle, _ptr(self.consts_t), self._cstride, _ptr(self.data_t),
+                               _ptr(self.lower_bound_t), _ptr(self.upper_bound_t), self._bstride,
+                               float(tol), float(mu), float(eta), float(acc), float(dec),
+                               _ptr(self.pars_t), _ptr(self.step_t), _ptr(self.lam_t), _ptr(self.step_type_t),
+                               _ptr(self.f_t), _ptr(self.first_f), _ptr(self.last_f), _ptr(self.iters_t),
+                               self.Nprobs, int(iters), proto if self._cstride == 0 else None,
+                               len(self._protocol or []), lbh if self._bstride == 0 else None,
+                               ubh if self._bstride == 0 else None, int(block), ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_lm_run", rc)
+        return None
+
+
+class F:
+    """Accumulating objective f += sum_i (m - d_i)^2 (reference ``F``, lsqnonlin.py:119-199)."""
+
+    def __init__(self, *args, **kwargs):
+        model_expr, _unused, legacy, ndata, dtype, write_to_file = _parse_ctor(
+            args, kwargs, ("model_expr", "ndata", "dtype", "write_to_file"))
+        self.dtype = _dtype(dtype)
+        src, struct, P, C, tag, mexpr = _model_from(model_expr, None, legacy)
+        self.nparam, self.nconst, self.ndata = P, C, int(ndata)
+        self.funcid = _funcid("f", P, C, self.ndata, self.dtype, tag)
+        self._source, self._struct = src, struct
+        self._prog = None
+
+    def build(self):
+        if self._prog is None or self._prog.device != torch.cuda.current_device():
+            self._prog = _Program.get(self._source, self._struct, self.nparam, self.nconst, self.ndata, self.dtype,
+                                      self.dtype)
+        return self._prog
+
+    def run(self, pars, consts, data, step_type, f):
+        pars, consts, data, f = (_as_tensor(x, n) for x, n in ((pars, "pars"), (consts, "consts"),
+                                                              (data, "data"), (f, "f")))
+        N = int(pars.shape[1])
+        if tuple(data.shape) != (self.ndata, N) or f.numel() != N:
+            raise RuntimeError("shape mismatch between pars, data and f")
+        st = None
+        if step_type is not None:
+            st = _as_tensor(step_type, "step_type")
+            if st.dtype != torch.int8 or st.numel() != N:
+                st = None if st.numel() != N else st.to(torch.int8)
+        consts, cstride, proto = _shared_rows(consts, self.nconst * self.ndata, N, "consts", True)
+        with torch.cuda.device(pars.device):
+            prog = self.build()
+            pv = (ctypes.c_double * max(1, len(proto or [])))(*(proto or [0.0]))
+            rc = _lib.lib().pcgb_f_run(prog.handle, _ptr(pars), _ptr(consts), cstride, _ptr(data), _ptr(st), _ptr(f),
+                                       N, pv if cstride == 0 else None, len(proto or []),
+                                       ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_f_run", rc)
+
+
+class GMW81Solver:
+    """Batched GMW81 modified-Cholesky solver (reference ``GMW81Solver``, solver.py:490-595)."""
+
+    def __init__(self, ndim: int, dtype=torch.float32, write_to_file: bool = False):
+        self.ndim = int(ndim)
+        self.dtype = _dtype(dtype)
+        names = [f"x{k}" for k in range(self.ndim)]
+        gm = codegen.generate("+".join(names), names, [], struct_name=f"GmwShape{self.ndim}")
+        self._source, self._struct = gm.source, gm.struct_name
+        self._prog = None
+
+    def run(self, mat, rhs, step_type=None, sol=None):
+        mat, rhs, sol = _as_tensor(mat, "mat"), _as_tensor(rhs, "rhs"), _as_tensor(sol, "sol")
+        n, N = int(rhs.shape[0]), int(rhs.shape[1])
+        if n != self.ndim or tuple(mat.shape) != (n * (n + 1) // 2, N) or tuple(sol.shape) != (n, N):
+            raise RuntimeError("mat must be (ndim*(ndim+1)/2, N), rhs and sol (ndim, N)")
+        for t in (mat, rhs, sol):
+            if t.dtype != self.dtype or not t.is_contiguous() or not t.is_cuda:
+                raise RuntimeError("mat, rhs, sol must be contiguous CUDA tensors of the solver dtype")
+        with torch.cuda.device(mat.device):
+            if self._prog is None or self._prog.device != torch.cuda.current_device():
+                self._prog = _Program.get(self._source, self._struct, self.ndim, 0, 1, self.dtype, self.dtype)
+            rc = _lib.lib().pcgb_gmw81_solve(self._prog.handle, _ptr(mat), _ptr(rhs), _ptr(sol), N,
+                                             ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_gmw81_solve", rc)

@@ -1,0 +1,83 @@
+"""libpcgb.so: loads without a GPU, exports every entry point of include/pcgb.h,
+compiles fitter programs with NVRTC for sm_103a, and rejects bad arguments
+with an error code and message instead of crashing."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from pycompute_gb300 import _lib, codegen, synth
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    names = []
+    for fn in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if fn.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", fn)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names += re.findall(r"\b(pcgb_[a-z0-9_]+)\s*\(", text)
+    return sorted(set(names))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.lib()
+    declared = _declared()
+    assert len(declared) >= 10
+    for name in declared:
+        assert hasattr(L, name), name
+    assert set(declared) == set(_lib.SIGNATURES), "ctypes signatures out of sync with the header"
+
+
+def test_version_and_limits():
+    L = _lib.lib()
+    assert b"sm_103a" in L.pcgb_version()
+    assert L.pcgb_max_params() == 8
+    assert L.pcgb_max_protocol() >= 64
+
+
+def _compile(gm, M, dt=0, sdt=1):
+    L = _lib.lib()
+    buf = ctypes.create_string_buffer(1 << 16)
+    rc = L.pcgb_fitter_compile(gm.source.encode(), gm.struct_name.encode(), gm.P, gm.C, M, dt, sdt,
+                               _lib.cache_dir().encode(), buf, len(buf))
+    return rc, buf.value.decode(), L.pcgb_last_error().decode()
+
+
+def test_nvrtc_compiles_ivim_for_sm103a_without_spills():
+    w = synth.ivim()
+    gm = codegen.generate(w.expr, w.pars, w.consts)
+    for dt, sdt in ((0, 1), (0, 0), (1, 1)):
+        rc, log, err = _compile(gm, w.M, dt, sdt)
+        assert rc == 0, err
+        if log:  # empty when served from the cubin cache
+            blk = log.split("Function properties for pcgb_lm_c1_b1")[1].split("Compiling")[0]
+            assert "0 bytes spill stores" in blk
+
+
+def test_compile_errors_are_reported():
+    rc, _, err = _compile(codegen.GeneratedModel(expr="x", pars=["a"], consts=[], struct_name="Nope",
+                                                 source="struct Nope { this is not C++ };", jnz=[True],
+                                                 hnz=[False]), 4)
+    assert rc == -1001 and "NVRTC" in err
+
+
+@pytest.mark.parametrize("P,C,M,dt,sdt,code", [
+    (0, 1, 10, 0, 1, -34), (9, 1, 10, 0, 1, -34), (4, 1, 0, 0, 1, -34), (4, 2, 200, 0, 1, -34),
+    (4, 1, 10, 2, 1, -22), (4, 1, 10, 1, 0, -22)])
+def test_create_argument_validation(P, C, M, dt, sdt, code):
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    rc = L.pcgb_fitter_create(b"struct X{};", b"X", P, C, M, dt, sdt, None, ctypes.byref(h))
+    assert rc == code and not h.value
+    assert L.pcgb_last_error()
+
+
+def test_run_rejects_null_fitter():
+    L = _lib.lib()
+    rc = L.pcgb_lm_run(None, None, 0, None, None, None, 0, 1e-8, .25, .75, .2, 2., None, None, None, None, None,
+                       None, None, None, 10, 10, None, 0, None, None, 0, None)
+    assert rc == -22 and b"NULL" in L.pcgb_last_error()
+    assert L.pcgb_fitter_destroy(None) == 0

@@ -1,0 +1,226 @@
+"""GPU fitter parity: the sm_103a kernels (through libpcgb.so's C ABI, via the
+drop-in classes) against the golden fixtures of the reference's own kernel and
+against the CPU oracle on the same seeded inputs.
+
+Tolerances (see pycompute_gb300.parity for why they are statistical after the
+first iteration):
+* 1 iteration: parameters within 1e-5 relative, step codes identical;
+* full runs: median relative error <= 1e-5 (fp32 state) / 1e-9 (fp64 state);
+  fraction of voxels beyond 1e-4 no worse than the CPU-vs-reference fp32 noise
+  floor plus a margin; convergence flags agree on >= 99.9 % of voxels
+  (>= 99.5 % on 512-voxel fixtures).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import OracleModel
+from pycompute_gb300 import Expr, F, GMW81Solver, SecondOrderLevenbergMarquardt, parity, synth
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+DEV = "cuda:0"
+
+
+def _gold(name):
+    z = np.load(os.path.join(GOLD, name))
+    return {k: z[k] for k in z.files}
+
+
+def _t(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.to(DEV)
+
+
+def fit_gpu(w, data, init, lb, ub, prot, iters, dtype=torch.float32, solve_dtype=None, per_voxel=False, **run_kw):
+    N = data.shape[1]
+    solm = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, dtype, solve_dtype=solve_dtype)
+    if per_voxel:
+        consts = _t(np.broadcast_to(prot[:, None], (len(prot), N)), dtype)
+        lbt = _t(np.broadcast_to(lb[:, None], (len(lb), N)), dtype)
+        ubt = _t(np.broadcast_to(ub[:, None], (len(ub), N)), dtype)
+        solm.detect_shared = False
+    else:
+        consts, lbt, ubt = _t(prot, dtype), _t(lb, dtype), _t(ub, dtype)
+    solm.setup(_t(init, dtype), consts, _t(data, dtype), lbt, ubt)
+    solm.run(iters, **run_kw)
+    torch.cuda.synchronize()
+    out = dict(pars=solm.pars_t.cpu().numpy(), step_type=solm.step_type_t.cpu().numpy()[0],
+               lam=solm.lam_t.cpu().numpy()[0], f=solm.f_t.cpu().numpy()[0], first_f=solm.first_f.cpu().numpy()[0],
+               last_f=solm.last_f.cpu().numpy()[0], step=solm.step_t.cpu().numpy(),
+               iters=solm.iters_t.cpu().numpy()[0])
+    return out, solm
+
+
+@pytest.fixture(scope="module")
+def oracles():
+    cache = {}
+
+    def get(w):
+        key = (w.expr, tuple(w.pars), tuple(w.consts))
+        if key not in cache:
+            cache[key] = OracleModel(w.expr, w.pars, w.consts)
+        return cache[key]
+    return get
+
+
+@pytest.mark.parametrize("M", [21, 10])
+@pytest.mark.parametrize("solve", [torch.float32, torch.float64])
+def test_one_iteration_matches_reference_golden(M, solve):
+    g = _gold(f"ivim{M}_it1.npz")
+    w = synth.ivim(synth.IVIM_B21 if M == 21 else synth.IVIM_B10)
+    out, _ = fit_gpu(w, g["data"], g["init"], g["lb"], g["ub"], g["protocol"], 1, solve_dtype=solve)
+    np.testing.assert_array_equal(out["step_type"], g["step_type"])
+    assert parity.compare_params(out["pars"], g["pars"])["max_rel"] < 1e-5
+    for k in ("first_f", "last_f", "f", "lam"):
+        np.testing.assert_allclose(out[k], g[k], rtol=1e-5)
+    assert np.all(out["iters"] == 1)
+
+
+@pytest.mark.parametrize("M", [21, 10])
+def test_full_fit_matches_reference_golden(M, oracles):
+    g = _gold(f"ivim{M}_it100.npz")
+    w = synth.ivim(synth.IVIM_B21 if M == 21 else synth.IVIM_B10)
+    # noise floor: the fp32 restatement on the CPU against the same golden run
+    p_cpu = g["init"].copy()
+    oracles(w).lm_run(p_cpu, g["protocol"], g["data"], g["lb"], g["ub"], 100)
+    floor = parity.compare_params(p_cpu, g["pars"])["frac_gt_1e-4"]
+    for solve in (torch.float32, torch.float64):
+        out, _ = fit_gpu(w, g["data"], g["init"], g["lb"], g["ub"], g["protocol"], 100, solve_dtype=solve)
+        rep = parity.compare_params(out["pars"], g["pars"])
+        assert rep["median_rel"] < 1e-5, rep
+        assert rep["frac_gt_1e-4"] <= floor + 0.05, (rep, floor)
+        assert parity.flags_agree(out["step_type"], g["step_type"]) >= 0.995
+
+
+@pytest.mark.parametrize("dtype,solve,mode", [(torch.float32, torch.float32, None),
+                                              (torch.float32, torch.float64, np.float64),
+                                              (torch.float64, torch.float64, None)])
+def test_ivim10_large_vs_oracle(dtype, solve, mode, oracles):
+    w = synth.ivim()
+    true, data, init, lb, ub, prot = w.generate(65536, seed=11)
+    npdt = np.float64 if dtype == torch.float64 else np.float32
+    c = lambda a: a.astype(npdt)  # noqa: E731
+    p_cpu = c(init).copy()
+    o = oracles(w).lm_run(p_cpu, c(prot), c(data), c(lb), c(ub), 100, solve_dtype=mode)
+    out, _ = fit_gpu(w, c(data), c(init), c(lb), c(ub), c(prot), 100, dtype=dtype, solve_dtype=solve)
+    rep = parity.compare_params(out["pars"], p_cpu)
+    if dtype == torch.float64:
+        assert rep["median_rel"] < 1e-9, rep
+        assert rep["frac_gt_1e-4"] < 0.01, rep
+    else:
+        assert rep["median_rel"] < 1e-5, rep
+        assert rep["frac_gt_1e-4"] < 0.12, rep
+    assert parity.flags_agree(out["step_type"], o["step_type"]) >= 0.999
+    assert np.mean(out["iters"] == o["iters"]) > 0.9
+
+
+@pytest.mark.parametrize("wl", [synth.vfa_t1, synth.t2star, synth.biexp_t2, lambda: synth.ivim(synth.ivim_b16())],
+                         ids=["vfa8", "t2s16", "biexp32", "ivim16"])
+def test_other_models_vs_oracle(wl, oracles):
+    w = wl()
+    true, data, init, lb, ub, prot = w.generate(16384, seed=5)
+    p_cpu = init.copy()
+    o = oracles(w).lm_run(p_cpu, prot, data, lb, ub, 60, solve_dtype=np.float64)
+    out, _ = fit_gpu(w, data, init, lb, ub, prot, 60)
+    rep = parity.compare_params(out["pars"], p_cpu)
+    assert rep["median_rel"] < 1e-5, rep
+    assert rep["frac_gt_1e-4"] < 0.15, rep
+    assert parity.flags_agree(out["step_type"], o["step_type"]) >= 0.995
+
+
+@pytest.mark.parametrize("N", [1, 31, 33, 1025])
+def test_ragged_sizes(N, oracles):
+    w = synth.ivim()
+    true, data, init, lb, ub, prot = w.generate(N, seed=N)
+    p_cpu = init.copy()
+    o = oracles(w).lm_run(p_cpu, prot, data, lb, ub, 1, solve_dtype=np.float64)
+    out, _ = fit_gpu(w, data, init, lb, ub, prot, 1)
+    assert parity.compare_params(out["pars"], p_cpu)["max_rel"] < 1e-5
+    np.testing.assert_array_equal(out["step_type"], o["step_type"])
+
+
+def test_per_voxel_consts_and_bounds_match_shared():
+    w = synth.ivim()
+    true, data, init, lb, ub, prot = w.generate(4096, seed=3)
+    a, _ = fit_gpu(w, data, init, lb, ub, prot, 100)
+    b, _ = fit_gpu(w, data, init, lb, ub, prot, 100, per_voxel=True)
+    rep = parity.compare_params(b["pars"], a["pars"])
+    assert rep["median_rel"] == 0.0 or rep["median_rel"] < 1e-6, rep
+    assert parity.flags_agree(a["step_type"], b["step_type"]) >= 0.999
+
+
+def test_run_continues_state_and_zero_iters():
+    w = synth.ivim()
+    true, data, init, lb, ub, prot = w.generate(2048, seed=4)
+    a, _ = fit_gpu(w, data, init, lb, ub, prot, 60)
+    b, solm = fit_gpu(w, data, init, lb, ub, prot, 30)
+    solm.run(30)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(solm.pars_t.cpu().numpy(), a["pars"])
+    np.testing.assert_array_equal(solm.step_type_t.cpu().numpy()[0], a["step_type"])
+    np.testing.assert_array_equal(solm.iters_t.cpu().numpy()[0], a["iters"])
+    before = solm.pars_t.clone()
+    solm.run(0)
+    torch.cuda.synchronize()
+    assert torch.equal(before, solm.pars_t)
+
+
+def test_nonfinite_voxels_are_contained(oracles):
+    w = synth.ivim()
+    true, data, init, lb, ub, prot = w.generate(256, seed=8)
+    data[:, 3] = np.nan
+    data[2, 7] = np.inf
+    data[:, 9] = 0.0
+    p_cpu = init.copy()
+    o = oracles(w).lm_run(p_cpu, prot, data, lb, ub, 20, solve_dtype=np.float64)
+    out, _ = fit_gpu(w, data, init, lb, ub, prot, 20)
+    ok = np.ones(256, bool)
+    ok[[3, 7, 9]] = False
+    assert parity.compare_params(out["pars"][:, ok], p_cpu[:, ok])["median_rel"] < 1e-5
+    np.testing.assert_array_equal(out["step_type"][[3, 7]], o["step_type"][[3, 7]])
+    assert np.all(np.isfinite(out["pars"]))
+
+
+def test_f_objective_accumulates(oracles):
+    w = synth.ivim()
+    true, data, init, lb, ub, prot = w.generate(5000, seed=6)
+    f = torch.full((1, 5000), 3.0, device=DEV)
+    fobj = F(w.expr, w.pars, w.consts, w.M, torch.float32)
+    fobj.run(_t(init), _t(prot), _t(data), None, f)
+    torch.cuda.synchronize()
+    want = oracles(w).cost(init, prot, data, np.full(5000, 3.0, dtype=np.float32))
+    np.testing.assert_allclose(f.cpu().numpy()[0], want, rtol=1e-5)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_gmw81_solver_vs_oracle(dtype, oracles):
+    rng = np.random.default_rng(1)
+    n, N = 4, 3000
+    mats = rng.standard_normal((10, N))
+    rhs = rng.standard_normal((n, N))
+    npdt = np.float64 if dtype == torch.float64 else np.float32
+    want = oracles(synth.ivim()).gmw81_solve(mats.astype(npdt), rhs.astype(npdt))
+    sol = torch.zeros((n, N), dtype=dtype, device=DEV)
+    GMW81Solver(n, dtype).run(_t(mats, dtype), _t(rhs, dtype), None, sol)
+    torch.cuda.synchronize()
+    got = sol.cpu().numpy()
+    tol = 1e-9 if dtype == torch.float64 else 2e-3
+    rel = parity.rel_err(got, want)
+    assert np.median(rel) < tol * 1e-2 and np.quantile(rel, 0.99) < tol * 50
+
+
+def test_input_validation_raises():
+    w = synth.ivim()
+    true, data, init, lb, ub, prot = w.generate(64, seed=1)
+    solm = SecondOrderLevenbergMarquardt(w.expr, w.pars, w.consts, ndata=w.M, dtype=torch.float32)
+    with pytest.raises(RuntimeError):
+        solm.setup(_t(init, torch.float64), _t(prot), _t(data), _t(lb), _t(ub))
+    with pytest.raises(RuntimeError):
+        solm.setup(_t(init[:3]), _t(prot), _t(data), _t(lb), _t(ub))
+    with pytest.raises(RuntimeError):
+        solm.run(10)
