@@ -10,6 +10,7 @@ from __future__ import annotations
 import ctypes
 import hashlib
 import os
+import platform
 import subprocess
 import threading
 
@@ -29,12 +30,24 @@ def _codegen():
     return codegen
 
 
-def _compile_model(gm) -> str:
+def _flags(contract: bool) -> list[str]:
+    if not contract:
+        return list(_CXXFLAGS)
+    # same code with fused multiply-adds, as the GPU compiler contracts them:
+    # a second legitimate rounding of the same algorithm (noise-floor twin)
+    f = [x for x in _CXXFLAGS if x != "-ffp-contract=off"] + ["-ffp-contract=fast"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        f.append("-mfma")
+    return f
+
+
+def _compile_model(gm, contract: bool = False) -> str:
     with open(os.path.join(HERE, "lm_oracle.hpp")) as f:
         hdr = f.read()
     with open(os.path.join(HERE, "oracle_api.cpp")) as f:
         api = f.read()
-    key = hashlib.sha1((hdr + api + gm.source + " ".join(_CXXFLAGS)).encode()).hexdigest()[:16]
+    flags = _flags(contract)
+    key = hashlib.sha1((hdr + api + gm.source + " ".join(flags)).encode()).hexdigest()[:16]
     d = os.path.join(BUILD, key)
     so = os.path.join(d, "liboracle.so")
     with _lock:
@@ -45,7 +58,7 @@ def _compile_model(gm) -> str:
         with open(mh, "w") as f:
             f.write(gm.source)
         tmp = so + f".tmp{os.getpid()}"
-        cmd = ["g++", *_CXXFLAGS, f"-I{HERE}", f"-I{d}", f'-DPCGB_MODEL_FILE="model.h"',
+        cmd = ["g++", *flags, f"-I{HERE}", f"-I{d}", f'-DPCGB_MODEL_FILE="model.h"',
                f"-DPCGB_MODEL_STRUCT={gm.struct_name}", os.path.join(HERE, "oracle_api.cpp"), "-o", tmp]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -62,13 +75,18 @@ MODES = {("float32", "float32"): 0, ("float32", "float64"): 1, ("float64", "floa
 
 
 class OracleModel:
-    """CPU restatement of the reference LM for one model expression."""
+    """CPU restatement of the reference LM for one model expression.
 
-    def __init__(self, expr: str, pars: list[str], consts: list[str]):
+    ``contract=True`` builds the same code with fused multiply-adds: a second
+    legitimate rounding of the algorithm, used to measure the noise floor that
+    two correct implementations show against each other.
+    """
+
+    def __init__(self, expr: str, pars: list[str], consts: list[str], contract: bool = False):
         cg = _codegen()
         self.gm = cg.generate(expr, pars, consts)
         self.P, self.C, self.H = self.gm.P, self.gm.C, self.gm.H
-        self.lib = ctypes.CDLL(_compile_model(self.gm))
+        self.lib = ctypes.CDLL(_compile_model(self.gm, contract))
         L = self.lib
         L.oracle_lm_run.restype = ctypes.c_int
         L.oracle_lm_run.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, ctypes.c_long, ctypes.c_long] + \

@@ -173,7 +173,126 @@ PCGB_HD void gmw81_solve(const T (&A)[P * (P + 1) / 2], const T (&b)[P], T (&x)[
   for (int i = 0; i < P; ++i) x[rot<P>(i)] = y[i] / s[i];
 }
 
+// ---- FP64 solve for an FP32 fitter -----------------------------------------
+//
+// GB300 issues FP64 at 1/64 of the FP32 rate, so the FP64 GMW81 path is
+// written to spend the FP64 pipe on the factorisation and solve arithmetic
+// only:
+//  * the rotation and the Jacobi scaling of matrix and right-hand side are the
+//    reference's own fp32 operations (solver.py:441-451); the scaled system is
+//    then widened to FP64 exactly;
+//  * the factorisation and the two triangular solves run in FP64 with one
+//    correctly rounded reciprocal per pivot (__drcp_rn) in place of the
+//    reference's per-element divisions;
+//  * maxima and comparisons of non-negative doubles are taken on their bit
+//    patterns (integer pipe). Like the reference's `if (t > m) m = t`, a NaN
+//    candidate never wins;
+//  * the unscaling multiplies by the fp32 reciprocal of the scale factor.
+// Rounding therefore differs from a textbook FP64 division-based solve by a
+// few FP64 ulps (and by fp32 rounding in the scale factors, which precondition
+// the system and cancel out of the solution up to that rounding).
+
+PCGB_HD unsigned long long abs_bits(double x) {
+  return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7fffffffffffffffULL;
+}
+// m = max(m, |x|) on bit patterns, NaN skipped (bit patterns above +Inf).
+PCGB_HD void max_abs_bits(unsigned long long& m, double x) {
+  const unsigned long long b = abs_bits(x);
+  if (b <= 0x7ff0000000000000ULL && b > m) m = b;
+}
+PCGB_HD double from_bits(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
+
+// A: packed fp32 matrix (row i, column j <= i), b: fp32 right-hand side.
+template <int P>
+PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const float (&b)[P], double (&x)[P]) {
+  float s[P], r[P];
+  double c[P][P];
+  double y[P];
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    const int pi = rot<P>(i);
+    s[i] = sqrtf(fabsf(A[pk(pi, pi)]));
+    r[i] = 1.0f / s[i];
+    y[i] = double(b[pi] / s[i]);
+  }
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    const int pi = rot<P>(i);
+#pragma unroll
+    for (int j = 0; j <= i; ++j) {
+      const int pj = rot<P>(j);
+      const float a = pi >= pj ? A[pk(pi, pj)] : A[pk(pj, pi)];
+      c[i][j] = double(a / (s[i] * s[j]));
+    }
+  }
+  // gamma = max |diag|, nu = max |offdiag| / sqrt(P^2 - 1)  (solver.py:32-57)
+  unsigned long long gb = 0, nb = 0;
+#pragma unroll
+  for (int i = 0; i < P; ++i)
+#pragma unroll
+    for (int j = 0; j <= i; ++j) max_abs_bits(i == j ? gb : nb, c[i][j]);
+  const double gam = from_bits(gb);
+  const double nu = P > 1 ? from_bits(nb) * (1.0 / sqrt(double(P * P - 1))) : 0.0;
+  unsigned long long bb = 0x3CBCD2B297D889BCULL;  // 4e-16, solver.py:109
+  if (abs_bits(gam) > bb) bb = abs_bits(gam);
+  if (abs_bits(nu) > bb) bb = abs_bits(nu);
+  const double inv_beta2 = __drcp_rn(from_bits(bb));
+  const double gn = gam + nu;
+  const double delta = gn > 1.0 ? 4e-16 * gn : 4e-16;
+
+  double inv_d[P];
+  double Lr[P][P];
+#pragma unroll
+  for (int j = 0; j < P; ++j) {
+#pragma unroll
+    for (int q = 0; q < j; ++q) Lr[j][q] = c[j][q] * inv_d[q];
+#pragma unroll
+    for (int i = j + 1; i < P; ++i) {
+      double t = c[i][j];
+#pragma unroll
+      for (int q = 0; q < j; ++q) t = fma(-Lr[j][q], c[i][q], t);
+      c[i][j] = t;
+    }
+    unsigned long long tb = 0;
+#pragma unroll
+    for (int i = j + 1; i < P; ++i) max_abs_bits(tb, c[i][j]);
+    const double th = from_bits(tb);
+    const double th2 = (th * th) * inv_beta2;
+    // d = max(|c_jj|, delta, theta^2 / beta^2); a NaN c_jj falls through like the reference
+    const unsigned long long cj = abs_bits(c[j][j]);
+    double d = cj > 0x7ff0000000000000ULL ? c[j][j] : from_bits(cj);
+    if (abs_bits(d) < abs_bits(delta)) d = delta;
+    if (abs_bits(d) < abs_bits(th2)) d = th2;
+    inv_d[j] = __drcp_rn(d);
+#pragma unroll
+    for (int i = j + 1; i < P; ++i) c[i][i] = fma(-c[i][j], c[i][j] * inv_d[j], c[i][i]);
+  }
+  // L D y = b' with L_ij d_j = c_ij, then L^T z = y (solver.py:298-308, 341-350)
+#pragma unroll
+  for (int i = 0; i < P; ++i) {
+    double t = y[i];
+#pragma unroll
+    for (int j = 0; j < i; ++j) t = fma(-c[i][j], y[j], t);
+    y[i] = t * inv_d[i];
+  }
+#pragma unroll
+  for (int i = P - 1; i >= 0; --i) {
+    double t = y[i];
+#pragma unroll
+    for (int j = i + 1; j < P; ++j) t = fma(-Lr[j][i], y[j], t);
+    y[i] = t;
+  }
+#pragma unroll
+  for (int i = 0; i < P; ++i) x[rot<P>(i)] = y[i] * double(r[i]);
+}
+
 template <typename T> PCGB_HD T load(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
+
+template <typename A, typename B> struct SameType { static constexpr bool value = false; };
+template <typename A> struct SameType<A, A> { static constexpr bool value = true; };
+// FP32 state with the FP64 solve / gain-ratio path above
+template <typename TA, typename TS>
+constexpr bool kMixed = SameType<TA, float>::value && SameType<TS, double>::value;
 
 // All iterations of one voxel.
 template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
@@ -237,7 +356,22 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
     if (it == 0) first = f;
 
     // damped solve in TS (lsqnonlin.py:848-878), then drop NaN/Inf (881-891)
-    {
+    if constexpr (kMixed<TA, TS>) {
+      float A[H], b[P];
+      double x[P];
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        b[i] = g[i];
+#pragma unroll
+        for (int j = 0; j <= i; ++j) A[pk(i, j)] = i == j ? hd[i] : h[pk(i, j)];
+      }
+      gmw81_solve_f32in_f64<P>(A, b, x);
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        stp[k] = float(x[k]);
+        if (!isfinite(stp[k])) stp[k] = 0.0f;
+      }
+    } else {
       TS A[H], b[P], x[P];
 #pragma unroll
       for (int i = 0; i < P; ++i) {
@@ -289,7 +423,30 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
     }
 
     // gain ratio in TS (lsqnonlin.py:441-491)
-    {
+    bool accept, very_good, pred_neg;
+    if constexpr (kMixed<TA, TS>) {
+      // predicted = s.g - s^T h s / 2 and the test rho = actual / predicted > mu
+      // evaluated without the division: for predicted > 0 it is
+      // actual > mu * predicted; predicted == +0 gives rho = +Inf.
+      const double actual = 0.5 * (double(f) - double(ftp));
+      double sg = 0.0, q = 0.0;
+#pragma unroll
+      for (int i = 0; i < P; ++i) {
+        const double si = double(stp[i]);
+        double off = 0.0;
+#pragma unroll
+        for (int j = 0; j < i; ++j) off = fma(double(h[pk(i, j)]), double(stp[j]), off);
+        const double ti = fma(2.0, off, double(h[pk(i, i)]) * si);
+        q = fma(si, ti, q);
+        sg = fma(si, double(g[i]), sg);
+      }
+      const double pred = fma(-0.5, q, sg);
+      const bool pos = pred > 0.0;
+      const bool pzero = __double_as_longlong(pred) == 0;
+      accept = actual > 0.0 && ((pos && actual > double(mu) * pred) || pzero);
+      very_good = pzero || actual > double(eta) * pred;
+      pred_neg = pred < 0.0;
+    } else {
       const TS actual = TS(0.5) * (TS(f) - TS(ftp));
       TS pred = TS(0);
 #pragma unroll
@@ -303,23 +460,26 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
 #pragma unroll
       for (int i = 0; i < P; ++i) pred += TS(stp[i]) * TS(g[i]);
       const TS rho = actual / pred;
-      if ((rho > TS(mu)) && (actual > TS(0))) {
+      accept = (rho > TS(mu)) && (actual > TS(0));
+      very_good = rho > TS(eta);
+      pred_neg = pred < TS(0);
+    }
+    if (accept) {
 #pragma unroll
-        for (int k = 0; k < P; ++k) p[k] = pt[k];
-        if (rho > TS(eta)) {
-          lam *= acc;
-          st = 1;
-        } else {
-          st = 2;
-        }
+      for (int k = 0; k < P; ++k) p[k] = pt[k];
+      if (very_good) {
+        lam *= acc;
+        st = 1;
       } else {
-        lam *= dec;
-        st = 4;
+        st = 2;
       }
-      if (pred < TS(0)) {
-        lam *= dec;
-        st |= 8;
-      }
+    } else {
+      lam *= dec;
+      st = 4;
+    }
+    if (pred_neg) {
+      lam *= dec;
+      st |= 8;
     }
     // box projection (lsqnonlin.py:590-601)
 #pragma unroll

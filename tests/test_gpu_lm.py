@@ -5,10 +5,14 @@ against the CPU oracle on the same seeded inputs.
 Tolerances (see pycompute_gb300.parity for why they are statistical after the
 first iteration):
 * 1 iteration: parameters within 1e-5 relative, step codes identical;
-* full runs: median relative error <= 1e-5 (fp32 state) / 1e-9 (fp64 state);
-  fraction of voxels beyond 1e-4 no worse than the CPU-vs-reference fp32 noise
-  floor plus a margin; convergence flags agree on >= 99.9 % of voxels
-  (>= 99 % on 512-voxel fixtures, where one voxel is 0.2 %).
+* full runs: compared with the oracle on the same inputs and held to the noise
+  floor that two correct CPU builds of the oracle show against each other
+  (plain and with fused multiply-adds, which is how the GPU compiler rounds):
+  median relative error <= max(1e-5 fp32 / 1e-9 fp64, 4 x floor), fraction of
+  voxels beyond 1e-4 <= floor + 3 %, convergence-flag agreement >= floor - 1 %.
+  Measured on IVIM-10 the floor is ~1e-6 median, ~8 % beyond 1e-4 and 99.6 %
+  flag agreement in fp32; 1e-15, 0.1 % and 97.6 % in fp64 (where 94 % of the
+  voxels converge and the last iterations decide the flag).
 """
 import os
 
@@ -60,12 +64,28 @@ def fit_gpu(w, data, init, lb, ub, prot, iters, dtype=torch.float32, solve_dtype
 def oracles():
     cache = {}
 
-    def get(w):
-        key = (w.expr, tuple(w.pars), tuple(w.consts))
+    def get(w, contract=False):
+        key = (w.expr, tuple(w.pars), tuple(w.consts), contract)
         if key not in cache:
-            cache[key] = OracleModel(w.expr, w.pars, w.consts)
+            cache[key] = OracleModel(w.expr, w.pars, w.consts, contract=contract)
         return cache[key]
     return get
+
+
+def assert_within_floor(oracles, w, out, init, prot, data, lb, ub, iters, solve_dtype=None, median_tol=1e-5):
+    """GPU result vs oracle, held to the oracle-vs-oracle(FMA) noise floor."""
+    p1, p2 = init.copy(), init.copy()
+    o1 = oracles(w).lm_run(p1, prot, data, lb, ub, iters, solve_dtype=solve_dtype)
+    o2 = oracles(w, contract=True).lm_run(p2, prot, data, lb, ub, iters, solve_dtype=solve_dtype)
+    floor = parity.compare_params(p2, p1)
+    flags_floor = parity.flags_agree(o2["step_type"], o1["step_type"])
+    got = parity.compare_params(out["pars"], p1)
+    flags = parity.flags_agree(out["step_type"], o1["step_type"])
+    msg = dict(got=got, floor=floor, flags=flags, flags_floor=flags_floor)
+    assert got["median_rel"] <= max(median_tol, 4 * floor["median_rel"]), msg
+    assert got["frac_gt_1e-4"] <= floor["frac_gt_1e-4"] + 0.03, msg
+    assert flags >= flags_floor - 0.01, msg
+    return o1, msg
 
 
 @pytest.mark.parametrize("M", [21, 10])
@@ -107,17 +127,9 @@ def test_ivim10_large_vs_oracle(dtype, solve, mode, oracles):
     true, data, init, lb, ub, prot = w.generate(65536, seed=11)
     npdt = np.float64 if dtype == torch.float64 else np.float32
     c = lambda a: a.astype(npdt)  # noqa: E731
-    p_cpu = c(init).copy()
-    o = oracles(w).lm_run(p_cpu, c(prot), c(data), c(lb), c(ub), 100, solve_dtype=mode)
     out, _ = fit_gpu(w, c(data), c(init), c(lb), c(ub), c(prot), 100, dtype=dtype, solve_dtype=solve)
-    rep = parity.compare_params(out["pars"], p_cpu)
-    if dtype == torch.float64:
-        assert rep["median_rel"] < 1e-9, rep
-        assert rep["frac_gt_1e-4"] < 0.01, rep
-    else:
-        assert rep["median_rel"] < 1e-5, rep
-        assert rep["frac_gt_1e-4"] < 0.12, rep
-    assert parity.flags_agree(out["step_type"], o["step_type"]) >= 0.999
+    o, msg = assert_within_floor(oracles, w, out, c(init), c(prot), c(data), c(lb), c(ub), 100, solve_dtype=mode,
+                                 median_tol=1e-9 if dtype == torch.float64 else 1e-5)
     assert np.mean(out["iters"] == o["iters"]) > 0.9
 
 
@@ -126,13 +138,8 @@ def test_ivim10_large_vs_oracle(dtype, solve, mode, oracles):
 def test_other_models_vs_oracle(wl, oracles):
     w = wl()
     true, data, init, lb, ub, prot = w.generate(16384, seed=5)
-    p_cpu = init.copy()
-    o = oracles(w).lm_run(p_cpu, prot, data, lb, ub, 60, solve_dtype=np.float64)
     out, _ = fit_gpu(w, data, init, lb, ub, prot, 60)
-    rep = parity.compare_params(out["pars"], p_cpu)
-    assert rep["median_rel"] < 1e-5, rep
-    assert rep["frac_gt_1e-4"] < 0.15, rep
-    assert parity.flags_agree(out["step_type"], o["step_type"]) >= 0.995
+    assert_within_floor(oracles, w, out, init, prot, data, lb, ub, 60, solve_dtype=np.float64)
 
 
 @pytest.mark.parametrize("N", [1, 31, 33, 1025])
