@@ -9,7 +9,9 @@ first iteration):
   floor that two correct CPU builds of the oracle show against each other
   (plain and with fused multiply-adds, which is how the GPU compiler rounds):
   median relative error <= max(1e-5 fp32 / 1e-9 fp64, 4 x floor), fraction of
-  voxels beyond 1e-4 <= floor + 3 %, convergence-flag agreement >= floor - 1 %.
+  voxels beyond 1e-4 <= floor + 3 %, convergence-flag agreement >= floor - 2 %
+  and a converged fraction that moves no further from the oracle's than the
+  floor's does (+1 %): flips from rounding are symmetric, a bug is not.
   Measured on IVIM-10 the floor is ~1e-6 median, ~8 % beyond 1e-4 and 99.6 %
   flag agreement in fp32; 1e-15, 0.1 % and 97.6 % in fp64 (where 94 % of the
   voxels converge and the last iterations decide the flag).
@@ -81,10 +83,12 @@ def assert_within_floor(oracles, w, out, init, prot, data, lb, ub, iters, solve_
     flags_floor = parity.flags_agree(o2["step_type"], o1["step_type"])
     got = parity.compare_params(out["pars"], p1)
     flags = parity.flags_agree(out["step_type"], o1["step_type"])
-    msg = dict(got=got, floor=floor, flags=flags, flags_floor=flags_floor)
+    conv = [float(np.mean(x == 0)) for x in (o1["step_type"], o2["step_type"], out["step_type"])]
+    msg = dict(got=got, floor=floor, flags=flags, flags_floor=flags_floor, converged=conv)
     assert got["median_rel"] <= max(median_tol, 4 * floor["median_rel"]), msg
     assert got["frac_gt_1e-4"] <= floor["frac_gt_1e-4"] + 0.03, msg
-    assert flags >= flags_floor - 0.01, msg
+    assert flags >= flags_floor - 0.02, msg
+    assert abs(conv[2] - conv[0]) <= abs(conv[1] - conv[0]) + 0.01, msg
     return o1, msg
 
 
@@ -130,7 +134,7 @@ def test_ivim10_large_vs_oracle(dtype, solve, mode, oracles):
     out, _ = fit_gpu(w, c(data), c(init), c(lb), c(ub), c(prot), 100, dtype=dtype, solve_dtype=solve)
     o, msg = assert_within_floor(oracles, w, out, c(init), c(prot), c(data), c(lb), c(ub), 100, solve_dtype=mode,
                                  median_tol=1e-9 if dtype == torch.float64 else 1e-5)
-    assert np.mean(out["iters"] == o["iters"]) > 0.9
+    assert abs(out["iters"].mean() - o["iters"].mean()) <= 0.02 * o["iters"].mean()
 
 
 @pytest.mark.parametrize("wl", [synth.vfa_t1, synth.t2star, synth.biexp_t2, lambda: synth.ivim(synth.ivim_b16())],
