@@ -128,6 +128,64 @@ int pcgb_f_run(pcgb_fitter* fitter, const void* params, const void* consts, int6
 int pcgb_gmw81_solve(pcgb_fitter* fitter, const void* mat, const void* rhs, void* sol, int64_t nprobs,
                      void* stream);
 
+/* ---- warm-start network (no reference counterpart) -------------------------
+ *
+ * The reference starts every fit from constant parameters or from a segmented
+ * log-linear fit (pycompute/cuda/lsq.py:18-26). These entry points train and
+ * run a 16 -> 128 -> 128 -> 128 -> P GELU network (bf16 weights, fp32
+ * accumulation, tensor cores) whose outputs replace that initialisation.
+ * Weight layout per layer: (rows x ld) row-major, ld = inputs + 8, with the
+ * bias in column `inputs` of the fp32 master copy. All pointers are device
+ * pointers unless noted.
+ */
+
+/* Last error of the network entry points on this host thread. */
+const char* pcgb_mlp_last_error(void);
+
+/* C = A * B with bf16 operands and fp32 accumulation on the tensor cores.
+ * a_layout 0: A is (M, K) row-major, 1: A is (K, M) row-major.
+ * b_layout 0: B is (N, K) row-major, 1: B is (K, N) row-major.
+ * epilogue 0: z = C + bias -> out_f32, gelu(z) -> out_bf16
+ *          1: out_f32 = C + bias
+ *          2: out_bf16 = C * gelu'(zin)
+ *          3: out_f32 += C (atomic; allows split-K with k_split < K)
+ *          4: out_f32 = C
+ * K, lda, ldb must be multiples of 8. */
+int pcgb_gemm_bf16(int a_layout, int b_layout, int epilogue, const void* A, int64_t lda, const void* B, int64_t ldb,
+                   int64_t M, int64_t N, int64_t K, int64_t k_split, const float* bias, int64_t bias_stride,
+                   float* out_f32, int64_t ldo, void* out_bf16, int64_t ldob, const float* zin, int64_t ldz,
+                   void* stream);
+
+/* Mean-squared-error gradient dy = 2 (y - t) / (batch * nout) (bf16, zero in
+ * padding columns nout..ncols-1) and loss_sum += mean squared error. */
+int pcgb_mlp_mse_grad(const float* y, const float* t, int64_t ldy, int64_t batch, int nout, int ncols, void* dy,
+                      int64_t lddy, float* loss_sum, void* stream);
+
+/* One Adam step over a (rows x ld) weight buffer; rows >= rows_live are
+ * padding. corr is a device array {1 - b1^t, 1 - b2^t, s}: the bias
+ * corrections of step t and a learning-rate scale (the step uses lr * s), read
+ * at run time so one captured CUDA graph replays every step. Clears grad and
+ * refreshes the bf16 copy. */
+int pcgb_adam_step(float* master, float* m, float* v, float* grad, void* w_bf16, int64_t rows, int64_t ld,
+                   int64_t rows_live, float lr, float b1, float b2, float eps, const float* corr, void* stream);
+
+/* Training inputs x_rows (n x ldx) bf16 = signals / max per voxel, column nin
+ * = 1; snorm[v] = that maximum. With params/targets, also the normalised
+ * targets (n x ldt): kind 0 p/snorm, 1 p, 2 log p, then (g - mean) / std.
+ * signals (nin, n) and params (nout, n) are structure-of-arrays; kinds, mean,
+ * stdv are device arrays of nout entries. */
+int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, void* x_rows, int64_t ldx, float* snorm,
+                     const float* params, int nout, const int* kinds, const float* mean, const float* stdv,
+                     float* targets, int64_t ldt, void* stream);
+
+/* Fused inference of all four layers: signals (nin, n) -> initial parameters
+ * out (nout, n), clamped to [lb, ub]. w_bf16 / w_master are host arrays of the
+ * four layers' device pointers; kinds, mean, stdv, lb, ub are host arrays of
+ * nout entries. nin must be 16. */
+int pcgb_mlp_forward(const float* signals, int64_t n, int nin, const void* const* w_bf16, const float* const* w_master,
+                     int nout, const int* kinds, const float* mean, const float* stdv, const float* lb,
+                     const float* ub, float* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -37,6 +37,17 @@ SIGNATURES = {
     "pcgb_f_run": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p,
                            c_int, c_void_p]),
     "pcgb_gmw81_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+    "pcgb_mlp_last_error": (c_char_p, []),
+    "pcgb_gemm_bf16": (c_int, [c_int, c_int, c_int, c_void_p, c_i64, c_void_p, c_i64, c_i64, c_i64, c_i64, c_i64,
+                               c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p]),
+    "pcgb_mlp_mse_grad": (c_int, [c_void_p, c_void_p, c_i64, c_i64, c_int, c_int, c_void_p, c_i64, c_void_p,
+                                  c_void_p]),
+    "pcgb_adam_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_i64, c_i64, ctypes.c_float,
+                               ctypes.c_float, ctypes.c_float, ctypes.c_float, c_void_p, c_void_p]),
+    "pcgb_mlp_prepare": (c_int, [c_void_p, c_i64, c_int, c_void_p, c_i64, c_void_p, c_void_p, c_int, c_void_p,
+                                 c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+    "pcgb_mlp_forward": (c_int, [c_void_p, c_i64, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 
@@ -70,7 +81,9 @@ def lib(build_if_missing: bool = True):
 
 def check(fn_name: str, rc: int):
     if rc != 0:
-        msg = lib().pcgb_last_error().decode(errors="replace")
+        L = lib()
+        err = L.pcgb_mlp_last_error if fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")) else L.pcgb_last_error
+        msg = err().decode(errors="replace")
         raise PcgbError(fn_name, rc, msg)
 
 

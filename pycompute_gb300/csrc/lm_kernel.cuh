@@ -202,6 +202,21 @@ PCGB_HD void max_abs_bits(unsigned long long& m, double x) {
 }
 PCGB_HD double from_bits(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
 
+// Exact float -> double widening on the integer pipe (the F2F instruction
+// issues on the FP64 pipe): rebias the exponent by 1023 - 127 = 896 and move
+// the 23-bit mantissa to the top of the 52-bit one. Zero keeps its sign;
+// subnormal, infinite and NaN inputs take the hardware conversion.
+PCGB_HD double widen(float x) {
+  const unsigned u = __float_as_uint(x);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e - 1u < 254u) {
+    const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0xfffffu);
+    return __hiloint2double(static_cast<int>(hi), static_cast<int>(u << 29));
+  }
+  if ((u << 1) == 0u) return __hiloint2double(static_cast<int>(u & 0x80000000u), 0);
+  return static_cast<double>(x);
+}
+
 // A: packed fp32 matrix (row i, column j <= i), b: fp32 right-hand side.
 template <int P>
 PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const float (&b)[P], double (&x)[P]) {
@@ -213,7 +228,7 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
     const int pi = rot<P>(i);
     s[i] = sqrtf(fabsf(A[pk(pi, pi)]));
     r[i] = 1.0f / s[i];
-    y[i] = double(b[pi] / s[i]);
+    y[i] = widen(b[pi] / s[i]);
   }
 #pragma unroll
   for (int i = 0; i < P; ++i) {
@@ -222,7 +237,7 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
     for (int j = 0; j <= i; ++j) {
       const int pj = rot<P>(j);
       const float a = pi >= pj ? A[pk(pi, pj)] : A[pk(pj, pi)];
-      c[i][j] = double(a / (s[i] * s[j]));
+      c[i][j] = widen(a / (s[i] * s[j]));
     }
   }
   // gamma = max |diag|, nu = max |offdiag| / sqrt(P^2 - 1)  (solver.py:32-57)
@@ -283,7 +298,7 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
     y[i] = t;
   }
 #pragma unroll
-  for (int i = 0; i < P; ++i) x[rot<P>(i)] = y[i] * double(r[i]);
+  for (int i = 0; i < P; ++i) x[rot<P>(i)] = y[i] * widen(r[i]);
 }
 
 template <typename T> PCGB_HD T load(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
@@ -428,22 +443,26 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
       // predicted = s.g - s^T h s / 2 and the test rho = actual / predicted > mu
       // evaluated without the division: for predicted > 0 it is
       // actual > mu * predicted; predicted == +0 gives rho = +Inf.
-      const double actual = 0.5 * (double(f) - double(ftp));
-      double sg = 0.0, q = 0.0;
+      // actual = (f - ftp) / 2 is exact in FP64, so its sign is the sign of f - ftp
+      const double actual = 0.5 * (widen(f) - widen(ftp));
+      double sg = 0.0, q = 0.0, sd[P];
+#pragma unroll
+      for (int i = 0; i < P; ++i) sd[i] = widen(stp[i]);
 #pragma unroll
       for (int i = 0; i < P; ++i) {
-        const double si = double(stp[i]);
         double off = 0.0;
 #pragma unroll
-        for (int j = 0; j < i; ++j) off = fma(double(h[pk(i, j)]), double(stp[j]), off);
-        const double ti = fma(2.0, off, double(h[pk(i, i)]) * si);
-        q = fma(si, ti, q);
-        sg = fma(si, double(g[i]), sg);
+        for (int j = 0; j < i; ++j) off = fma(widen(h[pk(i, j)]), sd[j], off);
+        const double ti = fma(2.0, off, widen(h[pk(i, i)]) * sd[i]);
+        q = fma(sd[i], ti, q);
+        sg = fma(sd[i], widen(g[i]), sg);
       }
       const double pred = fma(-0.5, q, sg);
-      const bool pos = pred > 0.0;
-      const bool pzero = __double_as_longlong(pred) == 0;
-      accept = actual > 0.0 && ((pos && actual > double(mu) * pred) || pzero);
+      const long long pb = __double_as_longlong(pred);
+      const bool pzero = pb == 0;                         // +0: rho = +Inf
+      const bool pos = pb > 0;                            // > +0 (NaN has the sign bit or is > +Inf bits)
+      const bool up = f > ftp;                            // actual > 0
+      accept = up && ((pos && pb < 0x7ff0000000000000LL && actual > double(mu) * pred) || pzero);
       very_good = pzero || actual > double(eta) * pred;
       pred_neg = pred < 0.0;
     } else {
