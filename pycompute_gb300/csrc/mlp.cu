@@ -472,6 +472,11 @@ int pcgb_gemm_bf16(int a_layout, int b_layout, int epilogue, const void* A, int6
   if (M < 0 || N < 0 || K < 0) return mlp_fail(PCGB_EINVAL, "negative GEMM size");
   if (K % 8 || lda % 8 || ldb % 8) return mlp_fail(PCGB_EINVAL, "K, lda and ldb must be multiples of 8");
   if (epilogue < 0 || epilogue > 4) return mlp_fail(PCGB_EINVAL, "unknown epilogue");
+  // every 16-byte operand chunk a tile reads must lie inside the stored rows
+  const int64_t m8 = (M + 7) / 8 * 8, n8 = (N + 7) / 8 * 8;
+  if ((a_layout == 0 && lda < K) || (a_layout != 0 && lda < m8) || (b_layout == 0 && ldb < K) ||
+      (b_layout != 0 && ldb < n8))
+    return mlp_fail(PCGB_EINVAL, "leading dimension smaller than the stored row");
   if (M == 0 || N == 0) return PCGB_OK;
   if (k_split <= 0 || k_split > K) k_split = K;
   if (k_split % BK) k_split = (k_split + BK - 1) / BK * BK;
