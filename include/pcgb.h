@@ -112,6 +112,19 @@ int pcgb_lm_run(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, 
                 void* stream);
 
 /*
+ * pcgb_lm_run restricted to the n_items voxels listed in vox_idx (int32
+ * device array of distinct voxel indices < nprobs); all other voxels are left
+ * untouched. Used to refit a compacted subset (the warm-start fallback) in
+ * one launch without gathering its data. No reference counterpart.
+ */
+int pcgb_lm_run_subset(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                       void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                       const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                       int block, const int32_t* vox_idx, int64_t n_items, void* stream);
+
+/*
  * Accumulating objective f[v] += sum_i (m(p_v; c_i) - d_i)^2, voxels whose
  * step_type is 0 skipped (step_type may be NULL). Replaces F.run
  * (lsqnonlin.py:137-145; kernel lsqnonlin.py:160-172).
@@ -119,6 +132,11 @@ int pcgb_lm_run(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, 
 int pcgb_f_run(pcgb_fitter* fitter, const void* params, const void* consts, int64_t consts_stride, const void* data,
                const int8_t* step_type, void* f, int64_t nprobs, const double* protocol_host, int protocol_len,
                void* stream);
+
+/* pcgb_f_run for the voxels listed in vox_idx only (no reference counterpart). */
+int pcgb_f_run_subset(pcgb_fitter* fitter, const void* params, const void* consts, int64_t consts_stride,
+                      const void* data, const int8_t* step_type, void* f, int64_t nprobs, const double* protocol_host,
+                      int protocol_len, const int32_t* vox_idx, int64_t n_items, void* stream);
 
 /*
  * Batched GMW81 modified-Cholesky solve of packed symmetric (H, N) matrices

@@ -34,6 +34,12 @@ SIGNATURES = {
                             c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                             c_void_p, c_void_p, c_i64, c_int, c_void_p, c_int, c_void_p, c_void_p, c_int,
                             c_void_p]),
+    "pcgb_lm_run_subset": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_double,
+                                   c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_int, c_void_p, c_int, c_void_p,
+                                   c_void_p, c_int, c_void_p, c_i64, c_void_p]),
+    "pcgb_f_run_subset": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64,
+                                  c_void_p, c_int, c_void_p, c_i64, c_void_p]),
     "pcgb_f_run": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p,
                            c_int, c_void_p]),
     "pcgb_gmw81_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),

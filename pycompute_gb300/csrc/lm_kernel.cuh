@@ -314,6 +314,16 @@ template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHAR
 PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
   constexpr int P = Model::P, H = Model::H, C = Model::C;
   const long long N = a.N;
+  if (a.step_type[v] == 0) {
+    // converged before this call (lsqnonlin.py:1000-1002): nothing changes,
+    // first_f / last_f are copies of f as in the reference's host loop
+    if (a.iters > 0) {
+      const TA f0 = load<TA>(a.f, v);
+      static_cast<TA*>(a.first_f)[v] = f0;
+      static_cast<TA*>(a.last_f)[v] = f0;
+    }
+    return;
+  }
   TA p[P], lo[P], hi[P], stp[P];
 #pragma unroll
   for (int k = 0; k < P; ++k) {
@@ -527,12 +537,13 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
   if (a.iters_done) a.iters_done[v] += done;
 }
 
-// Grid-stride schedule: thread t fits voxels t, t + T, t + 2T, ...
+// Grid-stride schedule: thread t fits work items t, t + T, t + 2T, ...; an
+// item is a voxel index, or an entry of the compacted list vox_idx.
 template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
 __device__ void lm_grid(const PcgbLmParams& a) {
   const long long T = (long long)gridDim.x * blockDim.x;
-  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.N; v += T)
-    lm_fit_voxel<Model, M, TA, TS, SHARED_C, SHARED_B>(a, v);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n_items; i += T)
+    lm_fit_voxel<Model, M, TA, TS, SHARED_C, SHARED_B>(a, a.vox_idx ? (long long)a.vox_idx[i] : i);
 }
 
 // Accumulating cost, the reference F kernel (lsqnonlin.py:157-177, 46-67):
@@ -541,7 +552,8 @@ template <class Model, int M, typename TA, bool SHARED_C>
 __device__ void cost_grid(const PcgbLmParams& a) {
   constexpr int P = Model::P, C = Model::C;
   const long long T = (long long)gridDim.x * blockDim.x;
-  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.N; v += T) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n_items; i += T) {
+    const long long v = a.vox_idx ? (long long)a.vox_idx[i] : i;
     if (a.step_type && a.step_type[v] == 0) continue;
     TA p[P];
 #pragma unroll
@@ -567,7 +579,7 @@ template <int P, typename T>
 __device__ void gmw81_grid(const PcgbLmParams& a) {
   constexpr int H = P * (P + 1) / 2;
   const long long T_ = (long long)gridDim.x * blockDim.x;
-  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.N; v += T_) {
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.n_items; v += T_) {
     T A[H], b[P], x[P];
 #pragma unroll
     for (int q = 0; q < H; ++q) A[q] = load<T>(a.consts, q * a.N + v);

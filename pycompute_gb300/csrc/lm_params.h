@@ -22,6 +22,8 @@ struct PcgbLmParams {
   void* step;              // (P, N) out or null
   int* iters_done;         // (N) in/out iteration counter or null
   unsigned int* work;      // voxel work counter of the persistent schedule (zeroed by the host) or null
+  const int* vox_idx;      // when set, work item i fits voxel vox_idx[i] (a compacted subset)
+  long long n_items;       // number of work items: N, or the length of vox_idx
   long long N;
   long long cstride;       // N: per-voxel constants; 0: protocol_* hold them
   long long bstride;       // N: per-voxel bounds; 0: shared_* hold them

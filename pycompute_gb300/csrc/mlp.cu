@@ -478,8 +478,9 @@ int pcgb_gemm_bf16(int a_layout, int b_layout, int epilogue, const void* A, int6
       (b_layout != 0 && ldb < n8))
     return mlp_fail(PCGB_EINVAL, "leading dimension smaller than the stored row");
   if (M == 0 || N == 0) return PCGB_OK;
-  if (k_split <= 0 || k_split > K) k_split = K;
-  if (k_split % BK) k_split = (k_split + BK - 1) / BK * BK;
+  if (k_split <= 0 || k_split >= K) k_split = K;
+  else if (k_split % BK) k_split = (k_split + BK - 1) / BK * BK;
+  if (k_split > K) k_split = K;
   if (k_split != K && epilogue != EPI_DW_ATOMIC) return mlp_fail(PCGB_EINVAL, "split-K needs the atomic epilogue");
   GemmArgs g{static_cast<const bf16*>(A), lda, static_cast<const bf16*>(B), ldb, M, N, K, k_split,
              bias, bias_stride, out_f32, ldo, static_cast<bf16*>(out_bf16), ldob, zin, ldz};

@@ -165,13 +165,13 @@ int grid_for(int64_t n, int block) {
   return int(g);
 }
 
-int launch(pcgb_fitter* ft, KernelSlot slot, const PcgbLmParams& prm, int64_t n, int block, void* stream) {
+int launch(pcgb_fitter* ft, KernelSlot slot, PcgbLmParams prm, int64_t n, int block, void* stream) {
   if (!ft->k[slot]) return fail(PCGB_EINVAL, "kernel %s missing from program", kKernelNames[slot]);
   if (block <= 0) block = kDefaultBlock;
   if (block > kMaxBlock || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to %d", kMaxBlock);
   if (n == 0) return PCGB_OK;
-  PcgbLmParams local = prm;
-  void* args[] = {&local};
+  if (!prm.vox_idx) prm.n_items = n;
+  void* args[] = {&prm};
   cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(ft->k[slot]), dim3(grid_for(n, block)),
                                    dim3(block), args, 0, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, kKernelNames[slot]);
@@ -312,12 +312,12 @@ int pcgb_fitter_destroy(pcgb_fitter* ft) {
 
 const char* pcgb_fitter_log(const pcgb_fitter* ft) { return ft ? ft->log.c_str() : ""; }
 
-int pcgb_lm_run(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
-                const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
-                double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type, void* f,
-                void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
-                const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host, int block,
-                void* stream) {
+static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                       void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                       const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                       int block, const int32_t* vox_idx, int64_t n_items, void* stream) {
   g_err.clear();
   if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
   if (nprobs < 0 || iters < 0) return fail(PCGB_EINVAL, "nprobs and iters must be >= 0");
@@ -361,12 +361,52 @@ int pcgb_lm_run(pcgb_fitter* ft, const void* consts, int64_t consts_stride, cons
   prm.dec = dec;
   const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_LM_C1_B1 : K_LM_C1_B0)
                                              : (bounds_stride == 0 ? K_LM_C0_B1 : K_LM_C0_B0);
+  if (vox_idx) {
+    if (n_items < 0) return fail(PCGB_EINVAL, "n_items must be >= 0");
+    prm.vox_idx = vox_idx;
+    prm.n_items = n_items;
+    return launch(ft, slot, prm, n_items, block, stream);
+  }
   return launch(ft, slot, prm, nprobs, block, stream);
 }
+
+int pcgb_lm_run(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type, void* f,
+                void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host, int block,
+                void* stream) {
+  return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
+                     params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
+                     protocol_len, lb_host, ub_host, block, nullptr, 0, stream);
+}
+
+int pcgb_lm_run_subset(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                       void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                       const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                       int block, const int32_t* vox_idx, int64_t n_items, void* stream) {
+  if (!vox_idx) return fail(PCGB_EINVAL, "vox_idx is NULL");
+  return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
+                     params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
+                     protocol_len, lb_host, ub_host, block, vox_idx, n_items, stream);
+}
+
+int pcgb_f_run_subset(pcgb_fitter* ft, const void* params, const void* consts, int64_t consts_stride,
+                      const void* data, const int8_t* step_type, void* f, int64_t nprobs, const double* protocol_host,
+                      int protocol_len, const int32_t* vox_idx, int64_t n_items, void* stream);
 
 int pcgb_f_run(pcgb_fitter* ft, const void* params, const void* consts, int64_t consts_stride, const void* data,
                const int8_t* step_type, void* f, int64_t nprobs, const double* protocol_host, int protocol_len,
                void* stream) {
+  return pcgb_f_run_subset(ft, params, consts, consts_stride, data, step_type, f, nprobs, protocol_host, protocol_len,
+                           nullptr, 0, stream);
+}
+
+int pcgb_f_run_subset(pcgb_fitter* ft, const void* params, const void* consts, int64_t consts_stride,
+                      const void* data, const int8_t* step_type, void* f, int64_t nprobs, const double* protocol_host,
+                      int protocol_len, const int32_t* vox_idx, int64_t n_items, void* stream) {
   g_err.clear();
   if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
   if (nprobs < 0) return fail(PCGB_EINVAL, "nprobs must be >= 0");
@@ -382,6 +422,12 @@ int pcgb_f_run(pcgb_fitter* ft, const void* params, const void* consts, int64_t 
   prm.step_type = const_cast<signed char*>(reinterpret_cast<const signed char*>(step_type));
   prm.f = f;
   prm.N = nprobs;
+  if (vox_idx) {
+    if (n_items < 0) return fail(PCGB_EINVAL, "n_items must be >= 0");
+    prm.vox_idx = vox_idx;
+    prm.n_items = n_items;
+    return launch(ft, consts_stride == 0 ? K_COST_C1 : K_COST_C0, prm, n_items, 0, stream);
+  }
   return launch(ft, consts_stride == 0 ? K_COST_C1 : K_COST_C0, prm, nprobs, 0, stream);
 }
 

