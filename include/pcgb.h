@@ -146,6 +146,48 @@ int pcgb_f_run_subset(pcgb_fitter* fitter, const void* params, const void* const
 int pcgb_gmw81_solve(pcgb_fitter* fitter, const void* mat, const void* rhs, void* sol, int64_t nprobs,
                      void* stream);
 
+/*
+ * Forward model out[i][v] = m(p_v; c_i) for all voxels and samples, (M, N).
+ * The reference's per-element evaluator (pycompute/cuda/symbolic.py:18-347,
+ * Eval) was never compiled at HEAD; this is its working counterpart, used for
+ * synthetic signals and fitted curves.
+ */
+int pcgb_model_eval(pcgb_fitter* fitter, const void* params, const void* consts, int64_t consts_stride, void* out,
+                    int64_t nprobs, const double* protocol_host, int protocol_len, void* stream);
+
+/* ---- fit pipeline (no reference counterpart) -------------------------------
+ * fp32 structure-of-arrays buffers; values/lb/ub are host arrays of nparam.
+ */
+
+/* Last error of the pipeline entry points on this host thread. */
+const char* pcgb_pipeline_last_error(void);
+
+/* Constant initialisation: pars[k][v] = values[k]; a NaN entry means "the
+ * voxel's largest sample" (the reference notebooks' S0 start). */
+int pcgb_init_constant(const float* data, int64_t n, int m, int nparam, const double* values, float* pars,
+                       void* stream);
+
+/* Flag voxels whose fit is not trusted (non-finite cost, cost not below
+ * cost_ref, or a parameter on a bound) and append their indices to idx
+ * (capacity n). count (one int32 on the device) must be zero on entry and
+ * receives the number of flagged voxels. flags may be NULL. */
+int pcgb_fallback_flags(const float* pars, const float* cost, const float* cost_ref, int64_t n, int nparam,
+                        const double* lb, const double* ub, int8_t* flags, int32_t* idx, int32_t* count,
+                        void* stream);
+
+/* For the n_items listed voxels: save pars (P, n_items) and cost into
+ * backup / cost_backup, write the constant initialisation (values as in
+ * pcgb_init_constant), reset lam to lam0, step_type to 1 and f to 0. */
+int pcgb_fallback_prepare(const int32_t* idx, int64_t n_items, int64_t n, int nparam, int m, const double* values,
+                          float* pars, float* backup, const float* cost, float* cost_backup, const float* data,
+                          float* lam, float lam0, int8_t* step_type, float* f, void* stream);
+
+/* Keep the refit of each listed voxel only if its cost is lower than the
+ * saved one, else restore the saved parameters and cost; which[v] (may be
+ * NULL) = 1 where the refit was kept. */
+int pcgb_fallback_select(const int32_t* idx, int64_t n_items, int64_t n, int nparam, float* pars,
+                         const float* backup, float* cost, const float* cost_backup, int8_t* which, void* stream);
+
 /* ---- warm-start network (no reference counterpart) -------------------------
  *
  * The reference starts every fit from constant parameters or from a segmented

@@ -43,6 +43,15 @@ SIGNATURES = {
     "pcgb_f_run": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p,
                            c_int, c_void_p]),
     "pcgb_gmw81_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+    "pcgb_model_eval": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_int, c_void_p]),
+    "pcgb_pipeline_last_error": (c_char_p, []),
+    "pcgb_init_constant": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "pcgb_fallback_flags": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_int, c_void_p, c_void_p, c_void_p,
+                                    c_void_p, c_void_p, c_void_p]),
+    "pcgb_fallback_prepare": (c_int, [c_void_p, c_i64, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_void_p, ctypes.c_float, c_void_p, c_void_p, c_void_p]),
+    "pcgb_fallback_select": (c_int, [c_void_p, c_i64, c_i64, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
+                                     c_void_p, c_void_p]),
     "pcgb_mlp_last_error": (c_char_p, []),
     "pcgb_gemm_bf16": (c_int, [c_int, c_int, c_int, c_void_p, c_i64, c_void_p, c_i64, c_i64, c_i64, c_i64, c_i64,
                                c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p]),
@@ -88,7 +97,12 @@ def lib(build_if_missing: bool = True):
 def check(fn_name: str, rc: int):
     if rc != 0:
         L = lib()
-        err = L.pcgb_mlp_last_error if fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")) else L.pcgb_last_error
+        if fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")):
+            err = L.pcgb_mlp_last_error
+        elif fn_name.startswith(("pcgb_init_constant", "pcgb_fallback")):
+            err = L.pcgb_pipeline_last_error
+        else:
+            err = L.pcgb_last_error
         msg = err().decode(errors="replace")
         raise PcgbError(fn_name, rc, msg)
 

@@ -572,6 +572,27 @@ __device__ void cost_grid(const PcgbLmParams& a) {
   }
 }
 
+// Forward model m(p_v; c_i) for every voxel and sample into model_out (M, N):
+// synthetic signals, residual maps, fitted curves.
+template <class Model, int M, typename TA, bool SHARED_C>
+__device__ void eval_grid(const PcgbLmParams& a) {
+  constexpr int P = Model::P, C = Model::C;
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.n_items; v += T) {
+    TA p[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * a.N + v);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      TA c[C > 0 ? C : 1];
+#pragma unroll
+      for (int k = 0; k < C; ++k)
+        c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : load<TA>(a.consts, (k * M + i) * a.cstride + v);
+      static_cast<TA*>(a.model_out)[i * a.N + v] = Model::template value<TA>(p, c);
+    }
+  }
+}
+
 // Batched GMW81 solve (the reference GMW81Solver kernel, solver.py:526-563):
 // consts holds the packed (H, N) matrices, data the (P, N) right-hand sides,
 // step receives the (P, N) solutions.

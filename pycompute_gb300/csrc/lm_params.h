@@ -20,6 +20,7 @@ struct PcgbLmParams {
   void* first_f;           // (N) out, cost after the first iteration of the call
   void* last_f;            // (N) out, cost after the last iteration of the call
   void* step;              // (P, N) out or null
+  void* model_out;         // (M, N) model values out (forward-model evaluation)
   int* iters_done;         // (N) in/out iteration counter or null
   unsigned int* work;      // voxel work counter of the persistent schedule (zeroed by the host) or null
   const int* vox_idx;      // when set, work item i fits voxel vox_idx[i] (a compacted subset)

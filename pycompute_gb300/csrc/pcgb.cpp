@@ -53,9 +53,12 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
   return h;
 }
 
-enum KernelSlot { K_LM_C1_B1, K_LM_C1_B0, K_LM_C0_B1, K_LM_C0_B0, K_COST_C1, K_COST_C0, K_GMW, K_COUNT };
+enum KernelSlot {
+  K_LM_C1_B1, K_LM_C1_B0, K_LM_C0_B1, K_LM_C0_B0, K_COST_C1, K_COST_C0, K_GMW, K_EVAL_C1, K_EVAL_C0, K_COUNT
+};
 const char* kKernelNames[K_COUNT] = {"pcgb_lm_c1_b1", "pcgb_lm_c1_b0", "pcgb_lm_c0_b1", "pcgb_lm_c0_b0",
-                                     "pcgb_cost_c1",  "pcgb_cost_c0",  "pcgb_gmw81"};
+                                     "pcgb_cost_c1",  "pcgb_cost_c0",  "pcgb_gmw81",    "pcgb_eval_c1",
+                                     "pcgb_eval_c0"};
 
 constexpr int kDefaultBlock = 128;
 constexpr int kMaxBlock = 256;
@@ -93,6 +96,10 @@ std::string program_source(const char* model_source, const char* model_struct, i
       << ">(a); }\n";
   s << "extern \"C\" __global__ void " << bounds << " pcgb_gmw81(const PcgbLmParams a) { pcgb::gmw81_grid<" << P
     << ", " << ts << ">(a); }\n";
+  for (int c = 1; c >= 0; --c)
+    s << "extern \"C\" __global__ void " << bounds << " pcgb_eval_c" << c
+      << "(const PcgbLmParams a) { pcgb::eval_grid<PcgbModel, " << M << ", " << ta << ", " << (c ? "true" : "false")
+      << ">(a); }\n";
   return s.str();
 }
 
@@ -429,6 +436,24 @@ int pcgb_f_run_subset(pcgb_fitter* ft, const void* params, const void* consts, i
     return launch(ft, consts_stride == 0 ? K_COST_C1 : K_COST_C0, prm, n_items, 0, stream);
   }
   return launch(ft, consts_stride == 0 ? K_COST_C1 : K_COST_C0, prm, nprobs, 0, stream);
+}
+
+int pcgb_model_eval(pcgb_fitter* ft, const void* params, const void* consts, int64_t consts_stride, void* out,
+                    int64_t nprobs, const double* protocol_host, int protocol_len, void* stream) {
+  g_err.clear();
+  if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
+  if (nprobs < 0) return fail(PCGB_EINVAL, "nprobs must be >= 0");
+  if (nprobs > 0 && (!params || !out)) return fail(PCGB_EINVAL, "params and out are required");
+  if (int rc = check_device(ft)) return rc;
+  PcgbLmParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  if (int rc = fill_protocol(ft, prm, consts_stride, nprobs, protocol_host, protocol_len)) return rc;
+  if (consts_stride != 0 && !consts) return fail(PCGB_EINVAL, "per-voxel consts pointer is NULL");
+  prm.pars = const_cast<void*>(params);
+  prm.consts = consts;
+  prm.model_out = out;
+  prm.N = nprobs;
+  return launch(ft, consts_stride == 0 ? K_EVAL_C1 : K_EVAL_C0, prm, nprobs, 0, stream);
 }
 
 int pcgb_gmw81_solve(pcgb_fitter* ft, const void* mat, const void* rhs, void* sol, int64_t nprobs, void* stream) {

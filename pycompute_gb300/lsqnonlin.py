@@ -310,6 +310,60 @@ class SecondOrderLevenbergMarquardt:
         return None
 
 
+    # ---- extensions used by the fit pipeline (no reference counterpart) -------
+    def _proto_args(self):
+        proto = (ctypes.c_double * max(1, len(self._protocol or [])))(*(self._protocol or [0.0]))
+        return proto if self._cstride == 0 else None, len(self._protocol or [])
+
+    def cost(self, pars_t=None, out=None, vox_idx=None, n_items=None) -> torch.Tensor:
+        """Cost sum_i (m(p) - d_i)^2 at ``pars_t`` (default: the current fit), (N,) fp."""
+        pars_t = self.pars_t if pars_t is None else pars_t
+        out = torch.zeros(self.Nprobs, dtype=self.dtype, device=pars_t.device) if out is None else out
+        with torch.cuda.device(pars_t.device):
+            prog = self.build()
+            pv, plen = self._proto_args()
+            if vox_idx is None:
+                rc = _lib.lib().pcgb_f_run(prog.handle, _ptr(pars_t), _ptr(self.consts_t), self._cstride,
+                                           _ptr(self.data_t), None, _ptr(out), self.Nprobs, pv, plen,
+                                           ctypes.c_void_p(_stream_ptr()))
+                _lib.check("pcgb_f_run", rc)
+            else:
+                rc = _lib.lib().pcgb_f_run_subset(prog.handle, _ptr(pars_t), _ptr(self.consts_t), self._cstride,
+                                                  _ptr(self.data_t), None, _ptr(out), self.Nprobs, pv, plen,
+                                                  _ptr(vox_idx), int(n_items), ctypes.c_void_p(_stream_ptr()))
+                _lib.check("pcgb_f_run_subset", rc)
+        return out
+
+    def run_subset(self, vox_idx: torch.Tensor, n_items: int, iters: int, tol=1e-8, mu=0.25, eta=0.75, acc=0.2,
+                   dec=2.0, block: int = 0):
+        """run() restricted to the voxels listed in ``vox_idx`` (int32, first n_items entries)."""
+        with torch.cuda.device(self.pars_t.device):
+            prog = self.build()
+            pv, plen = self._proto_args()
+            lbh = (ctypes.c_double * self.nparam)(*(self._lb_host or [0.0] * self.nparam))
+            ubh = (ctypes.c_double * self.nparam)(*(self._ub_host or [0.0] * self.nparam))
+            rc = _lib.lib().pcgb_lm_run_subset(
+                prog.handle, _ptr(self.consts_t), self._cstride, _ptr(self.data_t), _ptr(self.lower_bound_t),
+                _ptr(self.upper_bound_t), self._bstride, float(tol), float(mu), float(eta), float(acc), float(dec),
+                _ptr(self.pars_t), _ptr(self.step_t), _ptr(self.lam_t), _ptr(self.step_type_t), _ptr(self.f_t),
+                _ptr(self.first_f), _ptr(self.last_f), _ptr(self.iters_t), self.Nprobs, int(iters), pv, plen,
+                lbh if self._bstride == 0 else None, ubh if self._bstride == 0 else None, int(block),
+                _ptr(vox_idx), int(n_items), ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_lm_run_subset", rc)
+
+    def model_eval(self, pars_t: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Model values m(p_v; c_i), (M, N), with the protocol given to setup()."""
+        N = int(pars_t.shape[1])
+        out = torch.empty((self.ndata, N), dtype=self.dtype, device=pars_t.device) if out is None else out
+        with torch.cuda.device(pars_t.device):
+            prog = self.build()
+            pv, plen = self._proto_args()
+            rc = _lib.lib().pcgb_model_eval(prog.handle, _ptr(pars_t), _ptr(self.consts_t), self._cstride,
+                                            _ptr(out), N, pv, plen, ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_model_eval", rc)
+        return out
+
+
 class F:
     """Accumulating objective f += sum_i (m - d_i)^2 (reference ``F``, lsqnonlin.py:119-199)."""
 

@@ -1,0 +1,130 @@
+"""Fit pipeline on the GPU: synthetic signals, constant initialisation, and
+the warm-started fit with its plain-LM fallback.
+
+Warm-started fit (``WarmStartFitter.fit``):
+  1. the network predicts initial parameters from each voxel's signals;
+  2. the LM runs ``iters_warm`` iterations from there;
+  3. a voxel is flagged when its warm fit lands on a bound, has a non-finite
+     cost, or does not end below the cost of the constant initialisation
+     (the plain fitter's starting point);
+  4. flagged voxels are compacted into an index list and refitted by the
+     plain LM from the constant initialisation for ``iters_fallback``
+     iterations in one launch over that list;
+  5. each refitted voxel keeps whichever of the two fits has the lower cost.
+Every step is a kernel of libpcgb.so; PyTorch only holds the buffers.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from .lsqnonlin import Expr, SecondOrderLevenbergMarquardt
+from .synth import Workload
+
+
+def _p(t):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dvec(vals):
+    return (ctypes.c_double * len(vals))(*[float(v) for v in vals])
+
+
+def init_constant(data: torch.Tensor, values, out: torch.Tensor | None = None) -> torch.Tensor:
+    """(P, N) constant initial parameters; NaN entries take the voxel's largest sample."""
+    M, N = data.shape
+    P = len(values)
+    out = torch.empty((P, N), dtype=torch.float32, device=data.device) if out is None else out
+    rc = _lib.lib().pcgb_init_constant(_p(data), N, M, P, _dvec(values), _p(out), _stream())
+    _lib.check("pcgb_init_constant", rc)
+    return out
+
+
+def synth_gpu(w: Workload, n: int, seed: int, device="cuda", snr=None):
+    """Seeded synthetic signals on the GPU: (true params (P, n), signals (M, n)).
+
+    Parameters uniform in the workload's ranges, signals from the fitter's own
+    forward-model kernel, Rician magnitude noise with sigma = S0 / SNR.
+    """
+    dev = torch.device(device)
+    g = torch.Generator(device=dev).manual_seed(seed)
+    P, M = w.P, w.M
+    true = torch.empty((P, n), dtype=torch.float32, device=dev)
+    for k, (lo, hi) in enumerate(w.ranges):
+        true[k] = torch.rand(n, generator=g, device=dev) * (hi - lo) + lo
+    fitter = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, M, torch.float32)
+    prot = torch.tensor(w.protocol, dtype=torch.float32, device=dev)
+    lb = torch.tensor(w.lb, dtype=torch.float32, device=dev)
+    ub = torch.tensor(w.ub, dtype=torch.float32, device=dev)
+    dummy = torch.zeros((M, n), dtype=torch.float32, device=dev)
+    fitter.setup(true.clone(), prot, dummy, lb, ub)
+    clean = fitter.model_eval(true)
+    lo, hi = snr if snr is not None else w.snr
+    s = torch.rand(n, generator=g, device=dev) * (hi - lo) + lo if lo != hi else torch.full((n,), lo, device=dev)
+    sigma = true[0] / s
+    n1 = torch.randn((M, n), generator=g, device=dev)
+    n2 = torch.randn((M, n), generator=g, device=dev)
+    data = torch.sqrt((clean + sigma * n1) ** 2 + (sigma * n2) ** 2).contiguous()
+    return true, data
+
+
+class WarmStartFitter:
+    """Network initialisation + LM + plain-LM fallback (see module docstring)."""
+
+    def __init__(self, w: Workload, net, solve_dtype=torch.float64):
+        self.w = w
+        self.net = net
+        self.solve_dtype = solve_dtype
+        self.expr = Expr(w.expr, w.pars, w.consts)
+
+    def _fitter(self):
+        return SecondOrderLevenbergMarquardt(self.expr, None, self.w.M, torch.float32, solve_dtype=self.solve_dtype)
+
+    def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None):
+        w = self.w
+        dev = data.device
+        M, N = data.shape
+        P = w.P
+        prot = torch.tensor(w.protocol, dtype=torch.float32, device=dev)
+        lb = torch.tensor(w.lb, dtype=torch.float32, device=dev)
+        ub = torch.tensor(w.ub, dtype=torch.float32, device=dev)
+        pars = self.net.infer(data, out=pars_out)
+        solm = self._fitter()
+        solm.setup(pars, prot, data, lb, ub)
+        solm.run(iters_warm)
+        cost = solm.cost()
+        # cost at the plain fitter's starting point
+        p0 = init_constant(data, w.init_values)
+        cost0 = solm.cost(p0)
+        idx = torch.empty(N, dtype=torch.int32, device=dev)
+        count = torch.zeros(1, dtype=torch.int32, device=dev)
+        L = _lib.lib()
+        rc = L.pcgb_fallback_flags(_p(pars), _p(cost), _p(cost0), N, P, _dvec(w.lb), _dvec(w.ub), None, _p(idx),
+                                   _p(count), _stream())
+        _lib.check("pcgb_fallback_flags", rc)
+        nfb = int(count.item())
+        kept_refit = 0
+        if nfb:
+            backup = torch.empty((P, nfb), dtype=torch.float32, device=dev)
+            cost_b = torch.empty(nfb, dtype=torch.float32, device=dev)
+            rc = L.pcgb_fallback_prepare(_p(idx), nfb, N, P, M, _dvec(w.init_values), _p(pars), _p(backup), _p(cost),
+                                         _p(cost_b), _p(data), _p(solm.lam_t), 5.0, _p(solm.step_type_t),
+                                         _p(solm.f_t), _stream())
+            _lib.check("pcgb_fallback_prepare", rc)
+            solm.run_subset(idx, nfb, iters_fallback)
+            cost.index_fill_(0, idx[:nfb].long(), 0.0)
+            solm.cost(vox_idx=idx, n_items=nfb, out=cost)
+            which = torch.zeros(N, dtype=torch.int8, device=dev)
+            rc = L.pcgb_fallback_select(_p(idx), nfb, N, P, _p(pars), _p(backup), _p(cost), _p(cost_b), _p(which),
+                                        _stream())
+            _lib.check("pcgb_fallback_select", rc)
+            kept_refit = int(which.sum().item())
+        return dict(pars=pars, cost=cost, n_fallback=nfb, n_refit_kept=kept_refit, step_type=solm.step_type_t)

@@ -1,0 +1,104 @@
+"""Fit-pipeline kernels: constant initialisation, forward-model evaluation,
+the warm-start fallback, and what the trained network gains over the plain
+fit at the same iteration budget (median error against the all-FP64 fit)."""
+import numpy as np
+import pytest
+import torch
+
+from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, codegen, parity, pipeline, synth
+from pycompute_gb300.warmstart import WarmStartMLP
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda:0"
+
+
+def test_init_constant_and_model_eval():
+    w = synth.ivim()
+    true, data = pipeline.synth_gpu(w, 5000, seed=1, device=DEV)
+    p0 = pipeline.init_constant(data, w.init_values).cpu().numpy()
+    d = data.cpu().numpy()
+    np.testing.assert_array_equal(p0[0], d.max(axis=0))
+    np.testing.assert_array_equal(p0[1:], np.broadcast_to(np.array([0.1, 1e-2, 1e-3], np.float32)[:, None], (3, 5000)))
+    # forward model against an independent numpy evaluation
+    solm = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float32)
+    solm.setup(true.clone(), torch.tensor(w.protocol, device=DEV), data, torch.tensor(w.lb, device=DEV),
+               torch.tensor(w.ub, device=DEV))
+    m = solm.model_eval(true).cpu().numpy()
+    want = w.model_numpy(true.cpu().numpy().astype(np.float64), np.array(w.protocol))
+    np.testing.assert_allclose(m, want, rtol=2e-6)
+    # the Rician signals scatter around the model at the set SNR
+    resid = (d - want) / (true.cpu().numpy()[0] / 50.0)
+    assert 0.8 < resid.std() < 1.3
+
+
+def _fp64_fit(w, data, iters=1000):
+    solm = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float64)
+    p = pipeline.init_constant(data, w.init_values).double()
+    solm.setup(p, torch.tensor(w.protocol, device=DEV).double(), data.double(), torch.tensor(w.lb, device=DEV).double(),
+               torch.tensor(w.ub, device=DEV).double())
+    solm.run(iters, tol=1e-30)
+    torch.cuda.synchronize()
+    return p.cpu().numpy()
+
+
+def _plain_fit(w, data, iters):
+    solm = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float32)
+    p = pipeline.init_constant(data, w.init_values)
+    solm.setup(p, torch.tensor(w.protocol, device=DEV), data, torch.tensor(w.lb, device=DEV),
+               torch.tensor(w.ub, device=DEV))
+    solm.run(iters)
+    return p, solm.cost()
+
+
+class _BadNet:
+    """Stand-in network that returns a deliberately poor start for every 3rd voxel."""
+
+    def __init__(self, w):
+        self.w = w
+
+    def infer(self, data, out=None):
+        p = pipeline.init_constant(data, self.w.init_values)
+        p[:, ::3] = torch.tensor(self.w.ub, device=data.device)[:, None]  # on the upper bound
+        p[1, 1::3] = 0.9                                                    # far from the fit
+        if out is not None:
+            out.copy_(p)
+            return out
+        return p
+
+
+def test_fallback_refits_flagged_voxels():
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    true, data = pipeline.synth_gpu(w, 30000, seed=2, device=DEV)
+    res = pipeline.WarmStartFitter(w, _BadNet(w)).fit(data, iters_warm=3, iters_fallback=30)
+    torch.cuda.synchronize()
+    assert res["n_fallback"] >= 10000  # at least every 3rd voxel starts on a bound
+    p_plain, c_plain = _plain_fit(w, data, 30)
+    cost = res["cost"].cpu().numpy()
+    # every voxel ends at a cost no worse than the warm fit and, where it was
+    # refitted, no worse than the plain fit's
+    pars = res["pars"].cpu().numpy()
+    assert np.all(np.isfinite(pars))
+    refit = np.zeros(30000, bool)
+    refit[::3] = True
+    assert np.all(cost[refit] <= c_plain.cpu().numpy()[refit] * (1 + 1e-6) + 1e-3)
+
+
+def test_trained_network_beats_plain_lm_at_equal_iterations():
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    # training set: signals and the plain LM's fits of them as labels
+    _, tr_data = pipeline.synth_gpu(w, 1 << 18, seed=10, device=DEV)
+    labels, _ = _plain_fit(w, tr_data, 100)
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, DEV, seed=0)
+    net.train(tr_data, labels, epochs=12, batch=4096, lr=2e-3)
+    # evaluation set, unseen seed
+    _, data = pipeline.synth_gpu(w, 1 << 16, seed=11, device=DEV)
+    ref = _fp64_fit(w, data)
+    K = 3
+    p_plain, _ = _plain_fit(w, data, K)
+    res = pipeline.WarmStartFitter(w, net).fit(data, iters_warm=K, iters_fallback=30)
+    torch.cuda.synchronize()
+    e_plain = parity.compare_params(p_plain.cpu().numpy(), ref)["median_rel"]
+    e_warm = parity.compare_params(res["pars"].cpu().numpy(), ref)["median_rel"]
+    # the network start is worth several LM iterations
+    assert e_warm < 0.1 * e_plain, (e_warm, e_plain)
+    assert res["n_fallback"] < 0.2 * data.shape[1]
