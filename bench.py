@@ -156,6 +156,115 @@ def cpu_sample(iters: int, target_s: float, dtype_mode: str = "reference", min_v
     return n / el, kind, cores, sample
 
 
+def _median_rel_gpu(a, b):
+    """Median over voxels of the worst per-parameter relative error (on the GPU)."""
+    import torch
+    r = (a.double() - b.double()).abs() / b.double().abs().clamp_min(1e-30)
+    r = torch.nan_to_num(r, nan=float("inf")).amax(dim=0)
+    return float(r.median()), float((r > 1e-4).double().mean())
+
+
+def _time_ms(fn, warmup=2, reps=3):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(reps):
+        fn()
+    e.record()
+    torch.cuda.synchronize()
+    return s.elapsed_time(e) / reps
+
+
+def budget_for_tolerance(run_with, ref, budgets, tol=1e-4):
+    """Smallest iteration budget whose fit has median relative error <= tol vs ref."""
+    curve = {}
+    for k in budgets:
+        med, frac = _median_rel_gpu(run_with(k), ref)
+        curve[k] = (med, frac)
+        if med <= tol:
+            return k, curve
+    return None, curve
+
+
+def fp64_reference(w, data, iters=1000):
+    """All-FP64 fit (same LM, constant init, tolerance 1e-30) as the error reference."""
+    import torch
+    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline
+    dev = data.device
+    solm = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float64)
+    p = pipeline.init_constant(data, w.init_values).double()
+    solm.setup(p, torch.tensor(w.protocol, device=dev).double(), data.double(), torch.tensor(w.lb, device=dev).double(),
+               torch.tensor(w.ub, device=dev).double())
+    solm.run(iters, tol=1e-30)
+    torch.cuda.synchronize()
+    return p
+
+
+def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=8, seed=77):
+    """C5: IVIM-16, MLP warm start + LM + fallback vs plain LM, fits/s at 1e-4 vs FP64."""
+    import torch
+    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline, synth
+    from pycompute_gb300.warmstart import WarmStartMLP
+    dev = torch.device("cuda")
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    expr = Expr(w.expr, w.pars, w.consts)
+    prot = torch.tensor(w.protocol, device=dev)
+    lb = torch.tensor(w.lb, device=dev)
+    ub = torch.tensor(w.ub, device=dev)
+    t0 = time.perf_counter()
+    _, tr = pipeline.synth_gpu(w, n_train, seed=seed, device=dev)
+    lab = pipeline.init_constant(tr, w.init_values)
+    s = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32)
+    s.setup(lab, prot, tr, lb, ub)
+    s.run(100)
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, dev, seed=seed)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    net.train(tr, lab, epochs=epochs, batch=8192, lr=2e-3)
+    train_s = time.perf_counter() - t1
+    del tr, lab, s
+    _, data = pipeline.synth_gpu(w, n_eval, seed=seed + 1, device=dev)
+    ref = fp64_reference(w, data)
+    pars = torch.empty((4, n_eval), device=dev)
+    plain = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32)
+
+    def run_plain(k):
+        pipeline.init_constant(data, w.init_values, out=pars)
+        plain.setup(pars, prot, data, lb, ub)
+        plain.run(k)
+        return pars
+
+    wf = pipeline.WarmStartFitter(w, net)
+    state = {}
+
+    def run_warm(k):
+        state["res"] = wf.fit(data, iters_warm=k, iters_fallback=k_plain or 30, pars_out=pars)
+        return state["res"]["pars"]
+
+    k_plain, curve_plain = budget_for_tolerance(run_plain, ref, range(1, 31))
+    k_warm, curve_warm = budget_for_tolerance(run_warm, ref, range(0, 21))
+    out = {"workload": "ivim16_warm_vs_plain", "voxels": n_eval, "train_voxels": n_train, "epochs": epochs,
+           "train_s": round(train_s, 3), "setup_s": round(time.perf_counter() - t0, 1),
+           "plain_iters_for_1e-4": k_plain, "warm_iters_for_1e-4": k_warm,
+           "plain_curve": {k: v[0] for k, v in curve_plain.items()},
+           "warm_curve": {k: v[0] for k, v in curve_warm.items()}}
+    if k_plain is not None:
+        ms = _time_ms(lambda: run_plain(k_plain))
+        med, frac = _median_rel_gpu(run_plain(k_plain), ref)
+        out["plain"] = {"fits_per_s": n_eval / (ms / 1e3), "ms": ms, "median_rel_err": med, "frac_gt_1e-4": frac}
+    if k_warm is not None:
+        ms = _time_ms(lambda: run_warm(k_warm))
+        med, frac = _median_rel_gpu(run_warm(k_warm), ref)
+        out["warm"] = {"fits_per_s": n_eval / (ms / 1e3), "ms": ms, "median_rel_err": med, "frac_gt_1e-4": frac,
+                       "fallback_voxels": state["res"]["n_fallback"], "refits_kept": state["res"]["n_refit_kept"]}
+    if "plain" in out and "warm" in out:
+        out["speedup"] = out["warm"]["fits_per_s"] / out["plain"]["fits_per_s"]
+    return out
+
+
 def run_reference_arm(args):
     ws, rank, local = _dist()
     if rank != 0:
@@ -191,6 +300,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64-check", action="store_true")
+    ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison (IVIM-16)")
+    ap.add_argument("--warm-voxels", type=int, default=1 << 24)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
@@ -318,6 +429,27 @@ def main():
                "fp64_fit_s": round(t64, 3)}
         del p64, solm64
 
+    # ---- fits/s at the budget that reaches 1e-4 median error vs FP64 -------
+    at_tol = None
+    if not args.no_fp64_check:
+        ref64 = fp64_reference(w, data_d)
+
+        def run_k(k):
+            reset()
+            solm.run(k, block=args.block)
+            return pars_d
+
+        k_tol, curve = budget_for_tolerance(run_k, ref64, range(2, 41))
+        at_tol = {"iters": k_tol, "curve": {k: v[0] for k, v in curve.items()}}
+        if k_tol is not None:
+            ms = _time_ms(lambda: run_k(k_tol))
+            at_tol["fits_per_s"] = ws * N / (ms / 1e3)
+        del ref64
+
+    warm = None
+    if rank == 0 and ws == 1 and not args.no_warm:
+        warm = warm_start_comparison(n_eval=args.warm_voxels)
+
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -354,6 +486,8 @@ def main():
             "fit_stats": {"mean_iters": float(its.mean()), "converged_frac": float(np.mean(st == 0)),
                           "voxel_iters_per_s": float(its.sum()) * ws / (kern_ms / 1e3)},
             "accuracy": acc,
+            "at_1e-4_vs_fp64": at_tol,
+            "warm_start": warm,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": clk.summary(),

@@ -3,7 +3,9 @@ the warm-started fit with its plain-LM fallback.
 
 Warm-started fit (``WarmStartFitter.fit``):
   1. the network predicts initial parameters from each voxel's signals;
-  2. the LM runs ``iters_warm`` iterations from there;
+  2. the LM runs ``iters_warm`` iterations from there, starting with a small
+     damping ``lam0`` (the start is already close: the reference's lam = 5
+     would shrink the first steps to a sixth of a Gauss-Newton step);
   3. a voxel is flagged when its warm fit lands on a bound, has a non-finite
      cost, or does not end below the cost of the constant initialisation
      (the plain fitter's starting point);
@@ -88,7 +90,8 @@ class WarmStartFitter:
     def _fitter(self):
         return SecondOrderLevenbergMarquardt(self.expr, None, self.w.M, torch.float32, solve_dtype=self.solve_dtype)
 
-    def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None):
+    def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
+            lam0: float = 1e-3):
         w = self.w
         dev = data.device
         M, N = data.shape
@@ -99,6 +102,7 @@ class WarmStartFitter:
         pars = self.net.infer(data, out=pars_out)
         solm = self._fitter()
         solm.setup(pars, prot, data, lb, ub)
+        solm.lam_t.fill_(lam0)
         solm.run(iters_warm)
         cost = solm.cost()
         # cost at the plain fitter's starting point

@@ -101,7 +101,7 @@ def test_training_reduces_loss_and_graph_matches_eager():
         net.train(sig, lab, epochs=4, batch=B, lr=2e-3, use_graph=use_graph, log_every=8)
         nets.append(net)
     g, e = nets
-    assert g.losses[-1] < 0.5 * g.losses[0], g.losses
+    assert g.losses[-1] < 0.8 * g.losses[0] and all(np.diff(g.losses) < 0), g.losses
     # split-K weight gradients accumulate with atomics, so the two runs differ
     # in summation order only: same loss curve, nearly the same weights
     np.testing.assert_allclose(g.losses, e.losses, rtol=0.05)
