@@ -203,7 +203,7 @@ def fp64_reference(w, data, iters=1000):
     return p
 
 
-def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=8, seed=77):
+def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=24, seed=77, lam0=1e-3):
     """C5: IVIM-16, MLP warm start + LM + fallback vs plain LM, fits/s at 1e-4 vs FP64."""
     import torch
     from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline, synth
@@ -227,7 +227,7 @@ def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=8, seed=77):
     train_s = time.perf_counter() - t1
     del tr, lab, s
     _, data = pipeline.synth_gpu(w, n_eval, seed=seed + 1, device=dev)
-    ref = fp64_reference(w, data)
+    ref = fp64_reference(w, data, iters=300)
     pars = torch.empty((4, n_eval), device=dev)
     plain = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32)
 
@@ -240,8 +240,9 @@ def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=8, seed=77):
     wf = pipeline.WarmStartFitter(w, net)
     state = {}
 
-    def run_warm(k):
-        state["res"] = wf.fit(data, iters_warm=k, iters_fallback=k_plain or 30, pars_out=pars)
+    def run_warm(k, timings=None):
+        state["res"] = wf.fit(data, iters_warm=k, iters_fallback=k_plain or 30, pars_out=pars, lam0=lam0,
+                              timings=timings)
         return state["res"]["pars"]
 
     k_plain, curve_plain = budget_for_tolerance(run_plain, ref, range(1, 31))
@@ -258,8 +259,11 @@ def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=8, seed=77):
     if k_warm is not None:
         ms = _time_ms(lambda: run_warm(k_warm))
         med, frac = _median_rel_gpu(run_warm(k_warm), ref)
+        tm = {}
+        run_warm(k_warm, timings=tm)
         out["warm"] = {"fits_per_s": n_eval / (ms / 1e3), "ms": ms, "median_rel_err": med, "frac_gt_1e-4": frac,
-                       "fallback_voxels": state["res"]["n_fallback"], "refits_kept": state["res"]["n_refit_kept"]}
+                       "fallback_voxels": state["res"]["n_fallback"], "refits_kept": state["res"]["n_refit_kept"],
+                       "stage_ms": {k: round(v, 3) for k, v in tm.items()}}
     if "plain" in out and "warm" in out:
         out["speedup"] = out["warm"]["fits_per_s"] / out["plain"]["fits_per_s"]
     return out
@@ -302,9 +306,16 @@ def main():
     ap.add_argument("--no-fp64-check", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison (IVIM-16)")
     ap.add_argument("--warm-voxels", type=int, default=1 << 24)
+    ap.add_argument("--only-warm", action="store_true", help="run only the warm-start comparison")
+    ap.add_argument("--warm-epochs", type=int, default=24)
+    ap.add_argument("--warm-lam0", type=float, default=1e-3)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.only_warm:
+        print(json.dumps(warm_start_comparison(n_eval=args.warm_voxels, epochs=args.warm_epochs,
+                                               lam0=args.warm_lam0)), flush=True)
+        return 0
 
     import torch
     import torch.distributed as dist
@@ -448,7 +459,7 @@ def main():
 
     warm = None
     if rank == 0 and ws == 1 and not args.no_warm:
-        warm = warm_start_comparison(n_eval=args.warm_voxels)
+        warm = warm_start_comparison(n_eval=args.warm_voxels, epochs=args.warm_epochs, lam0=args.warm_lam0)
 
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
     cpu = None

@@ -309,45 +309,15 @@ template <typename A> struct SameType<A, A> { static constexpr bool value = true
 template <typename TA, typename TS>
 constexpr bool kMixed = SameType<TA, float>::value && SameType<TS, double>::value;
 
-// All iterations of one voxel.
-template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
-PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
+// The iterations of one voxel on register state (lsqnonlin.py:823-924 per
+// iteration). cf(k, i) returns constant k of sample i; first receives the cost
+// of the first iteration; done counts the iterations run.
+template <class Model, int M, typename TA, typename TS, class CF>
+PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const TA (&lo)[Model::P],
+                        const TA (&hi)[Model::P], TA (&stp)[Model::P], TA& lam, int& st, TA& f, TA& first, int& done,
+                        int iters, TA tol, TA mu, TA eta, TA acc, TA dec) {
   constexpr int P = Model::P, H = Model::H, C = Model::C;
-  const long long N = a.N;
-  if (a.step_type[v] == 0) {
-    // converged before this call (lsqnonlin.py:1000-1002): nothing changes,
-    // first_f / last_f are copies of f as in the reference's host loop
-    if (a.iters > 0) {
-      const TA f0 = load<TA>(a.f, v);
-      static_cast<TA*>(a.first_f)[v] = f0;
-      static_cast<TA*>(a.last_f)[v] = f0;
-    }
-    return;
-  }
-  TA p[P], lo[P], hi[P], stp[P];
-#pragma unroll
-  for (int k = 0; k < P; ++k) {
-    p[k] = load<TA>(a.pars, k * N + v);
-    lo[k] = SHARED_B ? Num<TA>::slb(a, k) : load<TA>(a.lb, k * a.bstride + v);
-    hi[k] = SHARED_B ? Num<TA>::sub(a, k) : load<TA>(a.ub, k * a.bstride + v);
-    stp[k] = a.step ? load<TA>(a.step, k * N + v) : TA(0);
-  }
-  TA d[M];
-#pragma unroll
-  for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
-  TA cv[SHARED_C ? 1 : (C > 0 ? C * M : 1)];
-  if (!SHARED_C) {
-#pragma unroll
-    for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
-  }
-  TA lam = load<TA>(a.lam, v);
-  int st = a.step_type[v];
-  TA f = load<TA>(a.f, v);
-  TA first = f;
-  const TA tol = TA(a.tol), mu = TA(a.mu), eta = TA(a.eta), acc = TA(a.acc), dec = TA(a.dec);
-  int done = 0;
-
-  for (int it = 0; it < a.iters; ++it) {
+  for (int it = 0; it < iters; ++it) {
     if (st == 0) break;
     ++done;
     // f, g = J^T r, h = sum (J J^T + r d2m), damped diagonal (lsqnonlin.py:225-256)
@@ -360,7 +330,7 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
     for (int i = 0; i < M; ++i) {
       TA c[C > 0 ? C : 1];
 #pragma unroll
-      for (int k = 0; k < C; ++k) c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : cv[k * M + i];
+      for (int k = 0; k < C; ++k) c[k] = cf(k, i);
       TA m, J[P], Hm[H];
       Model::template all<TA>(p, c, m, J, Hm);
       const TA r = m - d[i];
@@ -442,7 +412,7 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
     for (int i = 0; i < M; ++i) {
       TA c[C > 0 ? C : 1];
 #pragma unroll
-      for (int k = 0; k < C; ++k) c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : cv[k * M + i];
+      for (int k = 0; k < C; ++k) c[k] = cf(k, i);
       const TA r = Model::template value<TA>(pt, c) - d[i];
       ftp += r * r;
     }
@@ -518,6 +488,64 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
       else if (p[k] < lo[k])
         p[k] = lo[k];
     }
+  }
+
+}
+
+// protocol accessors for lm_iterate
+template <typename TA, int M> struct SharedConsts {
+  const PcgbLmParams& a;
+  PCGB_HD TA operator()(int k, int i) const { return Num<TA>::prot(a, k * M + i); }
+};
+template <typename TA, int M, int NC> struct RegConsts {
+  const TA (&cv)[NC];
+  PCGB_HD TA operator()(int k, int i) const { return cv[k * M + i]; }
+};
+
+// All iterations of one voxel.
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
+  constexpr int P = Model::P, H = Model::H, C = Model::C;
+  const long long N = a.N;
+  if (a.step_type[v] == 0) {
+    // converged before this call (lsqnonlin.py:1000-1002): nothing changes,
+    // first_f / last_f are copies of f as in the reference's host loop
+    if (a.iters > 0) {
+      const TA f0 = load<TA>(a.f, v);
+      static_cast<TA*>(a.first_f)[v] = f0;
+      static_cast<TA*>(a.last_f)[v] = f0;
+    }
+    return;
+  }
+  TA p[P], lo[P], hi[P], stp[P];
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    p[k] = load<TA>(a.pars, k * N + v);
+    lo[k] = SHARED_B ? Num<TA>::slb(a, k) : load<TA>(a.lb, k * a.bstride + v);
+    hi[k] = SHARED_B ? Num<TA>::sub(a, k) : load<TA>(a.ub, k * a.bstride + v);
+    stp[k] = a.step ? load<TA>(a.step, k * N + v) : TA(0);
+  }
+  TA d[M];
+#pragma unroll
+  for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
+  TA cv[SHARED_C ? 1 : (C > 0 ? C * M : 1)];
+  if (!SHARED_C) {
+#pragma unroll
+    for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
+  }
+  TA lam = load<TA>(a.lam, v);
+  int st = a.step_type[v];
+  TA f = load<TA>(a.f, v);
+  TA first = f;
+  const TA tol = TA(a.tol), mu = TA(a.mu), eta = TA(a.eta), acc = TA(a.acc), dec = TA(a.dec);
+  int done = 0;
+
+  if constexpr (SHARED_C) {
+    lm_iterate<Model, M, TA, TS>(SharedConsts<TA, M>{a}, d, p, lo, hi, stp, lam, st, f, first, done, a.iters, tol, mu,
+                                 eta, acc, dec);
+  } else {
+    lm_iterate<Model, M, TA, TS>(RegConsts<TA, M, (C > 0 ? C * M : 1)>{cv}, d, p, lo, hi, stp, lam, st, f, first,
+                                 done, a.iters, tol, mu, eta, acc, dec);
   }
 
   TA* pars = static_cast<TA*>(a.pars);

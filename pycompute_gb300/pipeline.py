@@ -91,7 +91,7 @@ class WarmStartFitter:
         return SecondOrderLevenbergMarquardt(self.expr, None, self.w.M, torch.float32, solve_dtype=self.solve_dtype)
 
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
-            lam0: float = 1e-3):
+            lam0: float = 1e-3, timings: dict | None = None):
         w = self.w
         dev = data.device
         M, N = data.shape
@@ -99,15 +99,28 @@ class WarmStartFitter:
         prot = torch.tensor(w.protocol, dtype=torch.float32, device=dev)
         lb = torch.tensor(w.lb, dtype=torch.float32, device=dev)
         ub = torch.tensor(w.ub, dtype=torch.float32, device=dev)
+        ev = []
+
+        def mark(name):
+            if timings is not None:
+                e = torch.cuda.Event(enable_timing=True)
+                e.record()
+                ev.append((name, e))
+
+        mark("start")
         pars = self.net.infer(data, out=pars_out)
+        mark("network")
         solm = self._fitter()
         solm.setup(pars, prot, data, lb, ub)
         solm.lam_t.fill_(lam0)
+        mark("setup")
         solm.run(iters_warm)
+        mark("lm_warm")
         cost = solm.cost()
         # cost at the plain fitter's starting point
         p0 = init_constant(data, w.init_values)
         cost0 = solm.cost(p0)
+        mark("costs")
         idx = torch.empty(N, dtype=torch.int32, device=dev)
         count = torch.zeros(1, dtype=torch.int32, device=dev)
         L = _lib.lib()
@@ -115,6 +128,7 @@ class WarmStartFitter:
                                    _p(count), _stream())
         _lib.check("pcgb_fallback_flags", rc)
         nfb = int(count.item())
+        mark("flags")
         kept_refit = 0
         if nfb:
             backup = torch.empty((P, nfb), dtype=torch.float32, device=dev)
@@ -131,4 +145,9 @@ class WarmStartFitter:
                                         _stream())
             _lib.check("pcgb_fallback_select", rc)
             kept_refit = int(which.sum().item())
+        mark("fallback")
+        if timings is not None:
+            torch.cuda.synchronize()
+            for (n0, e0), (n1, e1) in zip(ev[:-1], ev[1:]):
+                timings[n1] = timings.get(n1, 0.0) + e0.elapsed_time(e1)
         return dict(pars=pars, cost=cost, n_fallback=nfb, n_refit_kept=kept_refit, step_type=solm.step_type_t)
