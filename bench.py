@@ -203,7 +203,7 @@ def fp64_reference(w, data, iters=1000):
     return p
 
 
-def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=24, seed=77, lam0=1e-3):
+def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=64, seed=77, lam0=1e-3):
     """C5: IVIM-16, MLP warm start + LM + fallback vs plain LM, fits/s at 1e-4 vs FP64."""
     import torch
     from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline, synth
@@ -307,7 +307,7 @@ def main():
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison (IVIM-16)")
     ap.add_argument("--warm-voxels", type=int, default=1 << 24)
     ap.add_argument("--only-warm", action="store_true", help="run only the warm-start comparison")
-    ap.add_argument("--warm-epochs", type=int, default=24)
+    ap.add_argument("--warm-epochs", type=int, default=64)
     ap.add_argument("--warm-lam0", type=float, default=1e-3)
     args = ap.parse_args()
     if args.impl == "reference":

@@ -147,6 +147,31 @@ int pcgb_gmw81_solve(pcgb_fitter* fitter, const void* mat, const void* rhs, void
                      void* stream);
 
 /*
+ * One search step: f[v] += cost(p_v) (accumulating, like the reference's cost
+ * function), then (p_v, f[v]) replaces (best_p_v, best_f[v]) if f[v] is lower.
+ * Replaces SearchStep.run (lsqnonlin.py:1194-1199; kernel lsqnonlin.py:1153-1162).
+ */
+int pcgb_search_step(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data, const void* p,
+                     void* f, void* best_p, void* best_f, int64_t nprobs, const double* protocol_host,
+                     int protocol_len, void* stream);
+
+/*
+ * Random search in one launch: `draws` points per voxel uniform in [lb, ub],
+ * each refined by lm_iters LM iterations (from lambda = 5) when lm_iters > 0;
+ * best_p / best_f (in/out) keep the point of lowest cost. Draws come from a
+ * counter-based generator keyed by (seed, voxel, draw, parameter).
+ * Replaces RandomSearch.run (lsqnonlin.py:1232-1242, lm_iters = 0) and
+ * SecondOrderRandomSearch.run (lsqnonlin.py:1277-1291), which draw with
+ * cp.random on the host and launch once per draw. Each draw is compared by its
+ * own cost (the reference's cost buffer accumulates across draws).
+ */
+int pcgb_random_search(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, void* best_p,
+                       void* best_f, int64_t nprobs, int draws, int lm_iters, double tol, double mu, double eta,
+                       double acc, double dec, uint64_t seed, const double* protocol_host, int protocol_len,
+                       const double* lb_host, const double* ub_host, void* stream);
+
+/*
  * Forward model out[i][v] = m(p_v; c_i) for all voxels and samples, (M, N).
  * The reference's per-element evaluator (pycompute/cuda/symbolic.py:18-347,
  * Eval) was never compiled at HEAD; this is its working counterpart, used for

@@ -10,7 +10,6 @@ in column `in`.
 from __future__ import annotations
 
 import numpy as np
-from scipy.special import erf
 
 
 def bf16(x) -> np.ndarray:
@@ -20,12 +19,17 @@ def bf16(x) -> np.ndarray:
     return u.view(np.float32).astype(np.float64)
 
 
+_C = np.sqrt(2.0 / np.pi)
+
+
 def gelu(z):
-    return 0.5 * z * (1.0 + erf(z / np.sqrt(2.0)))
+    """GELU, tanh form (Hendrycks & Gimpel 2016), as the GPU kernels use it."""
+    return 0.5 * z * (1.0 + np.tanh(_C * (z + 0.044715 * z ** 3)))
 
 
 def gelu_grad(z):
-    return 0.5 * (1.0 + erf(z / np.sqrt(2.0))) + z * np.exp(-0.5 * z * z) / np.sqrt(2.0 * np.pi)
+    t = np.tanh(_C * (z + 0.044715 * z ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C * (1.0 + 3 * 0.044715 * z * z)
 
 
 def split(Wfull, fan_in, rows_live):

@@ -43,6 +43,11 @@ SIGNATURES = {
     "pcgb_f_run": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p,
                            c_int, c_void_p]),
     "pcgb_gmw81_solve": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+    "pcgb_search_step": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_i64,
+                                 c_void_p, c_int, c_void_p]),
+    "pcgb_random_search": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p,
+                                   c_void_p, c_i64, c_int, c_int, c_double, c_double, c_double, c_double, c_double,
+                                   ctypes.c_uint64, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "pcgb_model_eval": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_int, c_void_p]),
     "pcgb_pipeline_last_error": (c_char_p, []),
     "pcgb_init_constant": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p]),

@@ -27,6 +27,7 @@ fitter and the CPU oracle in both float and double.
 """
 from __future__ import annotations
 
+import functools
 import hashlib
 import re
 from dataclasses import dataclass, field
@@ -232,7 +233,14 @@ def _emit_block(exprs, names, prefix, indent="    "):
 
 
 def generate(expr: str, pars: list[str], consts: list[str], struct_name: str | None = None) -> GeneratedModel:
-    """Differentiate, CSE and print one model expression."""
+    """Differentiate, CSE and print one model expression (memoised: sympy
+    differentiation and CSE take tens of milliseconds per model)."""
+    return _generate_cached(expr, tuple(pars), tuple(consts), struct_name)
+
+
+@functools.lru_cache(maxsize=256)
+def _generate_cached(expr: str, pars: tuple, consts: tuple, struct_name: str | None) -> GeneratedModel:
+    pars, consts = list(pars), list(consts)
     if not pars:
         raise ValueError("a model needs at least one parameter")
     if len(pars) > 8:

@@ -621,6 +621,121 @@ __device__ void eval_grid(const PcgbLmParams& a) {
   }
 }
 
+// ---- searches ----------------------------------------------------------------
+
+// splitmix64 output function (Steele, Lea & Flood, OOPSLA 2014)
+PCGB_HD unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+// Counter-based uniform draw in [0, 1) with 24 random bits for component k of
+// draw d of voxel v: every voxel has an independent, reproducible stream.
+PCGB_HD float uniform01(unsigned long long seed, long long v, int d, int k) {
+  unsigned long long z = mix64(seed + 0x9E3779B97F4A7C15ULL * (unsigned long long)(v + 1));
+  z = mix64(z ^ (((unsigned long long)(unsigned)d << 8) | (unsigned)k));
+  return float(z >> 40) * (1.0f / 16777216.0f);
+}
+
+// One SearchStep launch (lsqnonlin.py:1083-1105, kernel 1153-1162): f[v] +=
+// cost(p_v) (accumulating, as the reference's cost function does), then keep
+// (p_v, f[v]) as the best point if f[v] < best_f[v].
+template <class Model, int M, typename TA, bool SHARED_C>
+__device__ void search_step_grid(const PcgbLmParams& a) {
+  constexpr int P = Model::P, C = Model::C;
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.n_items; v += T) {
+    TA p[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * a.N + v);
+    TA fa = TA(0);
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      TA c[C > 0 ? C : 1];
+#pragma unroll
+      for (int k = 0; k < C; ++k)
+        c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : load<TA>(a.consts, (k * M + i) * a.cstride + v);
+      const TA r = Model::template value<TA>(p, c) - load<TA>(a.data, i * a.N + v);
+      fa += r * r;
+    }
+    TA* f = static_cast<TA*>(a.f);
+    const TA fv = f[v] + fa;
+    f[v] = fv;
+    if (fv < load<TA>(a.best_f, v)) {
+#pragma unroll
+      for (int k = 0; k < P; ++k) static_cast<TA*>(a.best_p)[k * a.N + v] = p[k];
+      static_cast<TA*>(a.best_f)[v] = fv;
+    }
+  }
+}
+
+// Random search (RandomSearch.run, lsqnonlin.py:1232-1242) and, with
+// lm_iters > 0, second-order random search (SecondOrderRandomSearch.run,
+// lsqnonlin.py:1277-1291): a.iters draws uniform in [lb, ub]; each draw is
+// optionally refined by lm_iters LM iterations from lambda = 5, step_type = 1;
+// the draw's cost at its final point is compared with the best so far.
+// All draws of a voxel run in one thread with its signals in registers.
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+__device__ void random_search_grid(const PcgbLmParams& a) {
+  constexpr int P = Model::P, C = Model::C;
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x; v < a.n_items; v += T) {
+    const long long N = a.N;
+    TA lo[P], hi[P], bp[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      lo[k] = SHARED_B ? Num<TA>::slb(a, k) : load<TA>(a.lb, k * a.bstride + v);
+      hi[k] = SHARED_B ? Num<TA>::sub(a, k) : load<TA>(a.ub, k * a.bstride + v);
+      bp[k] = load<TA>(a.best_p, k * N + v);
+    }
+    TA d[M];
+#pragma unroll
+    for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
+    TA cv[SHARED_C ? 1 : (C > 0 ? C * M : 1)];
+    if (!SHARED_C) {
+#pragma unroll
+      for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
+    }
+    TA bf = load<TA>(a.best_f, v);
+    const TA tol = TA(a.tol), mu = TA(a.mu), eta = TA(a.eta), acc = TA(a.acc), dec = TA(a.dec);
+    for (int dr = 0; dr < a.iters; ++dr) {
+      TA p[P], stp[P];
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        p[k] = lo[k] + TA(uniform01(a.seed, v, dr, k)) * (hi[k] - lo[k]);
+        stp[k] = TA(0);
+      }
+      if (a.lm_iters > 0) {
+        TA lam = TA(5), f = TA(0), first = TA(0);
+        int st = 1, done = 0;
+        if constexpr (SHARED_C)
+          lm_iterate<Model, M, TA, TS>(SharedConsts<TA, M>{a}, d, p, lo, hi, stp, lam, st, f, first, done, a.lm_iters,
+                                       tol, mu, eta, acc, dec);
+        else
+          lm_iterate<Model, M, TA, TS>(RegConsts<TA, M, (C > 0 ? C * M : 1)>{cv}, d, p, lo, hi, stp, lam, st, f, first,
+                                       done, a.lm_iters, tol, mu, eta, acc, dec);
+      }
+      TA fa = TA(0);
+#pragma unroll
+      for (int i = 0; i < M; ++i) {
+        TA c[C > 0 ? C : 1];
+#pragma unroll
+        for (int k = 0; k < C; ++k) c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : cv[k * M + i];
+        const TA r = Model::template value<TA>(p, c) - d[i];
+        fa += r * r;
+      }
+      if (fa < bf) {
+        bf = fa;
+#pragma unroll
+        for (int k = 0; k < P; ++k) bp[k] = p[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < P; ++k) static_cast<TA*>(a.best_p)[k * N + v] = bp[k];
+    static_cast<TA*>(a.best_f)[v] = bf;
+  }
+}
+
 // Batched GMW81 solve (the reference GMW81Solver kernel, solver.py:526-563):
 // consts holds the packed (H, N) matrices, data the (P, N) right-hand sides,
 // step receives the (P, N) solutions.

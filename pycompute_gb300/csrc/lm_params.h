@@ -21,6 +21,10 @@ struct PcgbLmParams {
   void* last_f;            // (N) out, cost after the last iteration of the call
   void* step;              // (P, N) out or null
   void* model_out;         // (M, N) model values out (forward-model evaluation)
+  void* best_p;            // (P, N) best point of a search, in/out
+  void* best_f;            // (N) its cost, in/out
+  unsigned long long seed; // random-search draws: counter-based stream per (seed, voxel, draw)
+  int lm_iters;            // LM iterations per draw (0: plain random search)
   int* iters_done;         // (N) in/out iteration counter or null
   unsigned int* work;      // voxel work counter of the persistent schedule (zeroed by the host) or null
   const int* vox_idx;      // when set, work item i fits voxel vox_idx[i] (a compacted subset)

@@ -54,11 +54,13 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
 }
 
 enum KernelSlot {
-  K_LM_C1_B1, K_LM_C1_B0, K_LM_C0_B1, K_LM_C0_B0, K_COST_C1, K_COST_C0, K_GMW, K_EVAL_C1, K_EVAL_C0, K_COUNT
+  K_LM_C1_B1, K_LM_C1_B0, K_LM_C0_B1, K_LM_C0_B0, K_COST_C1, K_COST_C0, K_GMW, K_EVAL_C1, K_EVAL_C0,
+  K_SEARCH_C1, K_SEARCH_C0, K_RS_C1_B1, K_RS_C1_B0, K_RS_C0_B1, K_RS_C0_B0, K_COUNT
 };
 const char* kKernelNames[K_COUNT] = {"pcgb_lm_c1_b1", "pcgb_lm_c1_b0", "pcgb_lm_c0_b1", "pcgb_lm_c0_b0",
                                      "pcgb_cost_c1",  "pcgb_cost_c0",  "pcgb_gmw81",    "pcgb_eval_c1",
-                                     "pcgb_eval_c0"};
+                                     "pcgb_eval_c0",  "pcgb_search_c1", "pcgb_search_c0", "pcgb_rs_c1_b1",
+                                     "pcgb_rs_c1_b0", "pcgb_rs_c0_b1", "pcgb_rs_c0_b0"};
 
 constexpr int kDefaultBlock = 128;
 constexpr int kMaxBlock = 256;
@@ -96,6 +98,15 @@ std::string program_source(const char* model_source, const char* model_struct, i
       << ">(a); }\n";
   s << "extern \"C\" __global__ void " << bounds << " pcgb_gmw81(const PcgbLmParams a) { pcgb::gmw81_grid<" << P
     << ", " << ts << ">(a); }\n";
+  for (int c = 1; c >= 0; --c)
+    s << "extern \"C\" __global__ void " << bounds << " pcgb_search_c" << c
+      << "(const PcgbLmParams a) { pcgb::search_step_grid<PcgbModel, " << M << ", " << ta << ", "
+      << (c ? "true" : "false") << ">(a); }\n";
+  for (int c = 1; c >= 0; --c)
+    for (int b = 1; b >= 0; --b)
+      s << "extern \"C\" __global__ void " << bounds << " pcgb_rs_c" << c << "_b" << b
+        << "(const PcgbLmParams a) { pcgb::random_search_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
+        << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
   for (int c = 1; c >= 0; --c)
     s << "extern \"C\" __global__ void " << bounds << " pcgb_eval_c" << c
       << "(const PcgbLmParams a) { pcgb::eval_grid<PcgbModel, " << M << ", " << ta << ", " << (c ? "true" : "false")
@@ -454,6 +465,75 @@ int pcgb_model_eval(pcgb_fitter* ft, const void* params, const void* consts, int
   prm.model_out = out;
   prm.N = nprobs;
   return launch(ft, consts_stride == 0 ? K_EVAL_C1 : K_EVAL_C0, prm, nprobs, 0, stream);
+}
+
+int pcgb_search_step(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data, const void* p,
+                     void* f, void* best_p, void* best_f, int64_t nprobs, const double* protocol_host,
+                     int protocol_len, void* stream) {
+  g_err.clear();
+  if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
+  if (nprobs < 0) return fail(PCGB_EINVAL, "nprobs must be >= 0");
+  if (nprobs > 0 && (!data || !p || !f || !best_p || !best_f))
+    return fail(PCGB_EINVAL, "data, p, f, best_p and best_f are required");
+  if (int rc = check_device(ft)) return rc;
+  PcgbLmParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  if (int rc = fill_protocol(ft, prm, consts_stride, nprobs, protocol_host, protocol_len)) return rc;
+  if (consts_stride != 0 && !consts) return fail(PCGB_EINVAL, "per-voxel consts pointer is NULL");
+  prm.pars = const_cast<void*>(p);
+  prm.consts = consts;
+  prm.data = data;
+  prm.f = f;
+  prm.best_p = best_p;
+  prm.best_f = best_f;
+  prm.N = nprobs;
+  return launch(ft, consts_stride == 0 ? K_SEARCH_C1 : K_SEARCH_C0, prm, nprobs, 0, stream);
+}
+
+int pcgb_random_search(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, void* best_p,
+                       void* best_f, int64_t nprobs, int draws, int lm_iters, double tol, double mu, double eta,
+                       double acc, double dec, uint64_t seed, const double* protocol_host, int protocol_len,
+                       const double* lb_host, const double* ub_host, void* stream) {
+  g_err.clear();
+  if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
+  if (nprobs < 0 || draws < 0 || lm_iters < 0) return fail(PCGB_EINVAL, "nprobs, draws, lm_iters must be >= 0");
+  if (nprobs > 0 && (!data || !best_p || !best_f)) return fail(PCGB_EINVAL, "data, best_p and best_f are required");
+  if (int rc = check_device(ft)) return rc;
+  PcgbLmParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  if (int rc = fill_protocol(ft, prm, consts_stride, nprobs, protocol_host, protocol_len)) return rc;
+  if (consts_stride != 0 && !consts) return fail(PCGB_EINVAL, "per-voxel consts pointer is NULL");
+  if (bounds_stride == 0) {
+    if (!lb_host || !ub_host) return fail(PCGB_EINVAL, "shared bounds need lb_host and ub_host");
+    for (int k = 0; k < ft->P; ++k) {
+      prm.shared_lb_d[k] = lb_host[k];
+      prm.shared_ub_d[k] = ub_host[k];
+      prm.shared_lb_f[k] = float(lb_host[k]);
+      prm.shared_ub_f[k] = float(ub_host[k]);
+    }
+  } else if (bounds_stride != nprobs || !lower_bound || !upper_bound) {
+    return fail(PCGB_EINVAL, "bounds_stride must be 0 (shared) or nprobs with device bounds");
+  }
+  prm.consts = consts;
+  prm.data = data;
+  prm.lb = lower_bound;
+  prm.ub = upper_bound;
+  prm.bstride = bounds_stride;
+  prm.best_p = best_p;
+  prm.best_f = best_f;
+  prm.N = nprobs;
+  prm.iters = draws;
+  prm.lm_iters = lm_iters;
+  prm.seed = seed;
+  prm.tol = tol;
+  prm.mu = mu;
+  prm.eta = eta;
+  prm.acc = acc;
+  prm.dec = dec;
+  const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_RS_C1_B1 : K_RS_C1_B0)
+                                             : (bounds_stride == 0 ? K_RS_C0_B1 : K_RS_C0_B0);
+  return launch(ft, slot, prm, nprobs, 0, stream);
 }
 
 int pcgb_gmw81_solve(pcgb_fitter* ft, const void* mat, const void* rhs, void* sol, int64_t nprobs, void* stream) {

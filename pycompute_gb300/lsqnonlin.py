@@ -145,6 +145,22 @@ def _model_from(model_expr, f_gradf, legacy) -> tuple[str, str, int, int, str, O
     raise RuntimeError("One and only one of model_expr or f_gradf must be non None")
 
 
+_host_copies: dict = {}
+
+
+def _host_values(t: torch.Tensor) -> list:
+    """Host copy of a small shared protocol/bounds column, cached per tensor
+    version so repeated setup() calls with the same tensor need no sync."""
+    key = (t.data_ptr(), t.dtype, tuple(t.shape), t._version)
+    v = _host_copies.get(key)
+    if v is None:
+        v = t.reshape(-1).double().cpu().tolist()
+        if len(_host_copies) > 64:
+            _host_copies.clear()
+        _host_copies[key] = v
+    return v
+
+
 def _shared_rows(t: torch.Tensor, rows: int, n: int, name: str, detect: bool):
     """Classify a (rows, N) / (rows, 1) / (rows,) tensor: (tensor, stride, host values)."""
     if t.dim() == 1:
@@ -152,7 +168,7 @@ def _shared_rows(t: torch.Tensor, rows: int, n: int, name: str, detect: bool):
     if t.dim() != 2 or t.shape[0] != rows:
         raise RuntimeError(f"{name} must have {rows} rows, got shape {tuple(t.shape)}")
     if t.shape[1] == 1 and n != 1:
-        return t, 0, t[:, 0].double().cpu().tolist()
+        return t, 0, _host_values(t[:, 0])
     if t.shape[1] != n:
         raise RuntimeError(f"{name} must have 1 or {n} columns, got {t.shape[1]}")
     if detect and n > 0 and bool((t == t[:, :1]).all()):

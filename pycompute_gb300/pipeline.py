@@ -86,9 +86,21 @@ class WarmStartFitter:
         self.net = net
         self.solve_dtype = solve_dtype
         self.expr = Expr(w.expr, w.pars, w.consts)
+        self._solm = None
+        self._dev_consts = {}
 
     def _fitter(self):
-        return SecondOrderLevenbergMarquardt(self.expr, None, self.w.M, torch.float32, solve_dtype=self.solve_dtype)
+        if self._solm is None:
+            self._solm = SecondOrderLevenbergMarquardt(self.expr, None, self.w.M, torch.float32,
+                                                       solve_dtype=self.solve_dtype, detect_shared=False)
+        return self._solm
+
+    def _consts(self, dev):
+        if dev not in self._dev_consts:
+            w = self.w
+            self._dev_consts[dev] = tuple(torch.tensor(x, dtype=torch.float32, device=dev)
+                                          for x in (w.protocol, w.lb, w.ub))
+        return self._dev_consts[dev]
 
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
             lam0: float = 1e-3, timings: dict | None = None):
@@ -96,9 +108,7 @@ class WarmStartFitter:
         dev = data.device
         M, N = data.shape
         P = w.P
-        prot = torch.tensor(w.protocol, dtype=torch.float32, device=dev)
-        lb = torch.tensor(w.lb, dtype=torch.float32, device=dev)
-        ub = torch.tensor(w.ub, dtype=torch.float32, device=dev)
+        prot, lb, ub = self._consts(dev)
         ev = []
 
         def mark(name):

@@ -1,6 +1,6 @@
 """Learned warm start for the LM fitter.
 
-A 16 -> 128 -> 128 -> 128 -> P GELU network maps a voxel's signal curve to
+A 16 -> 128 -> 128 -> 128 -> P GELU (tanh form) network maps a voxel's signal curve to
 initial parameters. Weights are bf16 on the tensor cores with fp32 master
 copies and fp32 accumulation; training and inference run in libpcgb.so's
 hand-written kernels (csrc/mlp.cu): GEMMs with fused bias/GELU/GELU'
