@@ -94,6 +94,9 @@ class OracleModel:
         L.oracle_cost.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, ctypes.c_long] + [ctypes.c_void_p] * 4
         L.oracle_gmw81_solve.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long] + [ctypes.c_void_p] * 3
         L.oracle_set_threads.argtypes = [ctypes.c_int]
+        L.oracle_search_step.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, ctypes.c_long] + [ctypes.c_void_p] * 6
+        L.oracle_random_search.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_long, ctypes.c_long, ctypes.c_long] + \
+            [ctypes.c_void_p] * 6 + [ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong] + [ctypes.c_double] * 5
 
     def set_threads(self, n: int) -> int:
         return self.lib.oracle_set_threads(int(n))
@@ -154,6 +157,38 @@ class OracleModel:
         if rc != 0:
             raise RuntimeError(f"oracle_cost failed: {rc}")
         return f
+
+    def search_step(self, consts, data, p, f, best_p, best_f):
+        """SearchStep.run: f += cost(p); best_p / best_f updated in place."""
+        dt = p.dtype
+        P, N = p.shape
+        M = data.shape[0]
+        cstride = N if consts.ndim == 2 and consts.shape[1] == N and N != 1 else 0
+        consts = np.ascontiguousarray(consts.reshape(-1) if cstride == 0 else consts, dtype=dt)
+        rc = self.lib.oracle_search_step(int(dt == np.float64), M, N, cstride, _p(consts),
+                                         _p(np.ascontiguousarray(data, dtype=dt)), _p(np.ascontiguousarray(p)), _p(f),
+                                         _p(best_p), _p(best_f))
+        if rc != 0:
+            raise RuntimeError(f"oracle_search_step failed: {rc}")
+
+    def random_search(self, consts, data, lb, ub, best_p, best_f, draws, lm_iters=0, seed=0, tol=1e-8, mu=0.25,
+                      eta=0.75, acc=0.2, dec=2.0, solve_dtype=None):
+        """Random search (lm_iters = 0) or second-order random search; best_p / best_f in place."""
+        dt = best_p.dtype
+        sdt = np.dtype(solve_dtype) if solve_dtype is not None else dt
+        mode = MODES[(np.dtype(dt).name, sdt.name)]
+        P, N = best_p.shape
+        M = data.shape[0]
+        cstride = N if consts.ndim == 2 and consts.shape[1] == N and N != 1 else 0
+        consts = np.ascontiguousarray(consts.reshape(-1) if cstride == 0 else consts, dtype=dt)
+        bstride = N if lb.ndim == 2 and lb.shape[1] == N and N != 1 else 0
+        lb = np.ascontiguousarray(lb.reshape(-1) if bstride == 0 else lb, dtype=dt)
+        ub = np.ascontiguousarray(ub.reshape(-1) if bstride == 0 else ub, dtype=dt)
+        rc = self.lib.oracle_random_search(mode, M, N, cstride, bstride, _p(consts),
+                                           _p(np.ascontiguousarray(data, dtype=dt)), _p(lb), _p(ub), _p(best_p),
+                                           _p(best_f), int(draws), int(lm_iters), int(seed), tol, mu, eta, acc, dec)
+        if rc != 0:
+            raise RuntimeError(f"oracle_random_search failed: {rc}")
 
     def gmw81_solve(self, mat_packed, rhs):
         n, N = rhs.shape

@@ -405,4 +405,71 @@ void lm_voxel(long v, int M, const Strides& s, const RunParams& rp,
   if (iters_a) iters_a[v] += done;
 }
 
+// ---- searches ----------------------------------------------------------------
+
+// SearchStep (lsqnonlin.py:1083-1105): f += cost(p); keep p if f < best_f.
+template <class Model, typename TA>
+void search_step_voxel(long v, int M, const Strides& s, const TA* consts, const TA* data, const TA* p_a, TA* f_a,
+                       TA* best_p, TA* best_f) {
+  constexpr int P = Model::P;
+  TA p[P];
+  for (int k = 0; k < P; ++k) p[k] = p_a[k * s.N + v];
+  f_a[v] += cost<Model, TA>(p, consts, data, s, M, v);
+  if (f_a[v] < best_f[v]) {
+    for (int k = 0; k < P; ++k) best_p[k * s.N + v] = p[k];
+    best_f[v] = f_a[v];
+  }
+}
+
+// The draws of the GPU random search: splitmix64's output function (Steele,
+// Lea & Flood 2014) keyed by (seed, voxel, draw, component), 24-bit uniforms.
+inline unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+inline float uniform01(unsigned long long seed, long v, int d, int k) {
+  unsigned long long z = mix64(seed + 0x9E3779B97F4A7C15ULL * (unsigned long long)(v + 1));
+  z = mix64(z ^ (((unsigned long long)(unsigned)d << 8) | (unsigned)k));
+  return float(z >> 40) * (1.0f / 16777216.0f);
+}
+
+// RandomSearch.run / SecondOrderRandomSearch.run (lsqnonlin.py:1232-1242,
+// 1277-1291) for one voxel: each draw is rand * (ub - lb) + lb, optionally
+// refined by lm_iters LM iterations from lambda = 5, step_type = 1 (a fresh
+// setup, lsqnonlin.py:1288-1289), and compared by its own cost.
+template <class Model, typename TA, typename TS>
+void random_search_voxel(long v, int M, const Strides& s, const RunParams& rp, int draws, unsigned long long seed,
+                         const TA* consts, const TA* data, const TA* lb, const TA* ub, TA* best_p, TA* best_f) {
+  constexpr int P = Model::P, C = Model::C;
+  TA d[256], c[256], lo[P], hi[P];
+  for (int i = 0; i < M; ++i) d[i] = data[long(i) * s.N + v];
+  for (int k = 0; k < C; ++k)
+    for (int i = 0; i < M; ++i) c[k * M + i] = s.cstride ? consts[(long(k) * M + i) * s.cstride + v] : consts[k * M + i];
+  for (int k = 0; k < P; ++k) {
+    lo[k] = s.bstride ? lb[k * s.bstride + v] : lb[k];
+    hi[k] = s.bstride ? ub[k * s.bstride + v] : ub[k];
+  }
+  Strides one{1, 0, 0};
+  TA bf = best_f[v];
+  TA bp[P];
+  for (int k = 0; k < P; ++k) bp[k] = best_p[k * s.N + v];
+  for (int dr = 0; dr < draws; ++dr) {
+    TA p[P];
+    for (int k = 0; k < P; ++k) p[k] = std::fma(TA(uniform01(seed, v, dr, k)), hi[k] - lo[k], lo[k]);
+    if (rp.iters > 0) {
+      TA lam = TA(5), f = TA(0), ff = TA(0), lf = TA(0);
+      int8_t st = 1;
+      lm_voxel<Model, TA, TS>(0, M, one, rp, c, d, lo, hi, p, &lam, &st, &f, &ff, &lf, nullptr, nullptr);
+    }
+    const TA fc = cost<Model, TA>(p, c, d, one, M, 0);
+    if (fc < bf) {
+      bf = fc;
+      for (int k = 0; k < P; ++k) bp[k] = p[k];
+    }
+  }
+  for (int k = 0; k < P; ++k) best_p[k * s.N + v] = bp[k];
+  best_f[v] = bf;
+}
+
 }  // namespace oracle

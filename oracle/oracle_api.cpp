@@ -95,6 +95,48 @@ int oracle_cost(int dbl, int M, long N, long cstride, const void* pars, const vo
   return 0;
 }
 
+// One SearchStep over all voxels (f accumulates, best kept).
+int oracle_search_step(int dbl, int M, long N, long cstride, const void* consts, const void* data, const void* p,
+                       void* f, void* best_p, void* best_f) {
+  if (M <= 0 || N < 0) return -22;
+  oracle::Strides s{N, cstride, 0};
+#pragma omp parallel for schedule(static)
+  for (long v = 0; v < N; ++v) {
+    if (dbl)
+      oracle::search_step_voxel<Model, double>(v, M, s, (const double*)consts, (const double*)data, (const double*)p,
+                                               (double*)f, (double*)best_p, (double*)best_f);
+    else
+      oracle::search_step_voxel<Model, float>(v, M, s, (const float*)consts, (const float*)data, (const float*)p,
+                                              (float*)f, (float*)best_p, (float*)best_f);
+  }
+  return 0;
+}
+
+// Random search with optional LM refinement (mode as in oracle_lm_run).
+int oracle_random_search(int mode, int M, long N, long cstride, long bstride, const void* consts, const void* data,
+                         const void* lb, const void* ub, void* best_p, void* best_f, int draws, int lm_iters,
+                         unsigned long long seed, double tol, double mu, double eta, double acc, double dec) {
+  if (M <= 0 || M > 256 || N < 0 || draws < 0 || lm_iters < 0) return -22;
+  oracle::Strides s{N, cstride, bstride};
+  oracle::RunParams rp{lm_iters, tol, mu, eta, acc, dec};
+#pragma omp parallel for schedule(dynamic, 16)
+  for (long v = 0; v < N; ++v) {
+    if (mode == 0)
+      oracle::random_search_voxel<Model, float, float>(v, M, s, rp, draws, seed, (const float*)consts,
+                                                       (const float*)data, (const float*)lb, (const float*)ub,
+                                                       (float*)best_p, (float*)best_f);
+    else if (mode == 1)
+      oracle::random_search_voxel<Model, float, double>(v, M, s, rp, draws, seed, (const float*)consts,
+                                                        (const float*)data, (const float*)lb, (const float*)ub,
+                                                        (float*)best_p, (float*)best_f);
+    else
+      oracle::random_search_voxel<Model, double, double>(v, M, s, rp, draws, seed, (const double*)consts,
+                                                         (const double*)data, (const double*)lb, (const double*)ub,
+                                                         (double*)best_p, (double*)best_f);
+  }
+  return 0;
+}
+
 // Batched GMW81 solve of packed symmetric (H, N) matrices and (P, N) right-hand
 // sides, like the reference GMW81Solver kernel (solver.py:526-563).
 int oracle_gmw81_solve(int dbl, int n, long N, const void* mat, const void* rhs, void* sol) {

@@ -702,7 +702,7 @@ __device__ void random_search_grid(const PcgbLmParams& a) {
       TA p[P], stp[P];
 #pragma unroll
       for (int k = 0; k < P; ++k) {
-        p[k] = lo[k] + TA(uniform01(a.seed, v, dr, k)) * (hi[k] - lo[k]);
+        p[k] = fma(TA(uniform01(a.seed, v, dr, k)), hi[k] - lo[k], lo[k]);  // rand * (ub - lb) + lb
         stp[k] = TA(0);
       }
       if (a.lm_iters > 0) {

@@ -445,3 +445,102 @@ class GMW81Solver:
             rc = _lib.lib().pcgb_gmw81_solve(self._prog.handle, _ptr(mat), _ptr(rhs), _ptr(sol), N,
                                              ctypes.c_void_p(_stream_ptr()))
             _lib.check("pcgb_gmw81_solve", rc)
+
+
+class SearchStep:
+    """One cost-and-keep-best step (reference ``SearchStep``, lsqnonlin.py:1120-1199).
+
+    ``run(f, best_f, p, best_p)``: f += cost(p) (the reference's cost function
+    accumulates into f), then p replaces best_p where f < best_f.
+    """
+
+    def __init__(self, *args, **kwargs):
+        model_expr, _unused, legacy, ndata, dtype, write_to_file = _parse_ctor(
+            args, kwargs, ("model_expr", "ndata", "dtype", "write_to_file"))
+        if legacy is not None:
+            self._lm = SecondOrderLevenbergMarquardt(legacy[0], legacy[1], legacy[2], ndata=ndata, dtype=dtype)
+        else:
+            self._lm = SecondOrderLevenbergMarquardt(model_expr, None, ndata, dtype)
+        self.nparam, self.ndata, self.dtype = self._lm.nparam, self._lm.ndata, self._lm.dtype
+
+    def setup(self, consts_t, data_t, lower_bound_t, upper_bound_t):
+        N = int(_as_tensor(data_t, "data_t").shape[1])
+        dummy = torch.empty((self.nparam, N), dtype=self.dtype, device=_as_tensor(data_t, "data_t").device)
+        self._lm.setup(dummy, consts_t, data_t, lower_bound_t, upper_bound_t)
+        self.Nprobs = N
+
+    def run(self, f, best_f, p, best_p):
+        lm = self._lm
+        with torch.cuda.device(lm.data_t.device):
+            prog = lm.build()
+            pv, plen = lm._proto_args()
+            rc = _lib.lib().pcgb_search_step(prog.handle, _ptr(lm.consts_t), lm._cstride, _ptr(lm.data_t), _ptr(p),
+                                             _ptr(f), _ptr(best_p), _ptr(best_f), self.Nprobs, pv, plen,
+                                             ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_search_step", rc)
+
+
+class RandomSearch:
+    """Random search (reference ``RandomSearch``, lsqnonlin.py:1202-1242).
+
+    ``setup(consts, data, lb, ub)`` then ``run(iters)``: ``iters`` draws per
+    voxel uniform in [lb, ub], best point in ``best_pars_t`` / ``best_f_t``.
+    All draws run in one launch with a counter-based generator (``seed``);
+    each draw is compared by its own cost. (In the reference the cost buffer
+    accumulates across draws, lsqnonlin.py:1230-1242 with the accumulating
+    cost function, so in practice only its first draw is kept.) best_pars_t
+    starts at the lower bounds instead of uninitialised memory.
+    """
+
+    lm_iters = 0
+
+    def __init__(self, *args, solve_dtype=None, **kwargs):
+        model_expr, _unused, legacy, ndata, dtype, write_to_file = _parse_ctor(
+            args, kwargs, ("model_expr", "ndata", "dtype", "write_to_file"))
+        if legacy is not None:
+            self._lm = SecondOrderLevenbergMarquardt(legacy[0], legacy[1], legacy[2], ndata=ndata, dtype=dtype,
+                                                     solve_dtype=solve_dtype)
+        else:
+            self._lm = SecondOrderLevenbergMarquardt(model_expr, None, ndata, dtype, solve_dtype=solve_dtype)
+        self.nparam, self.ndata, self.dtype = self._lm.nparam, self._lm.ndata, self._lm.dtype
+        self._seed = 0x5EED5EED
+
+    def setup(self, consts_t, data_t, lower_bound_t, upper_bound_t):
+        data_t = _as_tensor(data_t, "data_t")
+        N = int(data_t.shape[1])
+        self.Nprobs = N
+        lbt = _as_tensor(lower_bound_t, "lower_bound_t")
+        self.best_pars_t = lbt.reshape(self.nparam, -1).expand(self.nparam, N).contiguous().clone()
+        self.best_f_t = torch.full((1, N), torch.finfo(self.dtype).max / 5, dtype=self.dtype, device=data_t.device)
+        self._lm.setup(self.best_pars_t.clone(), consts_t, data_t, lower_bound_t, upper_bound_t)
+
+    def run(self, iters: int, lm_iters: int | None = None, tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0,
+            seed: int | None = None):
+        lm = self._lm
+        lm_iters = self.lm_iters if lm_iters is None else int(lm_iters)
+        if seed is None:
+            self._seed = (self._seed + 0x9E3779B97F4A7C15) & 0xFFFFFFFFFFFFFFFF
+            seed = self._seed
+        with torch.cuda.device(lm.data_t.device):
+            prog = lm.build()
+            pv, plen = lm._proto_args()
+            lbh = (ctypes.c_double * self.nparam)(*(lm._lb_host or [0.0] * self.nparam))
+            ubh = (ctypes.c_double * self.nparam)(*(lm._ub_host or [0.0] * self.nparam))
+            rc = _lib.lib().pcgb_random_search(
+                prog.handle, _ptr(lm.consts_t), lm._cstride, _ptr(lm.data_t), _ptr(lm.lower_bound_t),
+                _ptr(lm.upper_bound_t), lm._bstride, _ptr(self.best_pars_t), _ptr(self.best_f_t), self.Nprobs,
+                int(iters), lm_iters, float(tol), float(mu), float(eta), float(acc), float(dec),
+                ctypes.c_uint64(int(seed)), pv, plen, lbh if lm._bstride == 0 else None,
+                ubh if lm._bstride == 0 else None, ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_random_search", rc)
+
+
+class SecondOrderRandomSearch(RandomSearch):
+    """Multi-start LM (reference ``SecondOrderRandomSearch``, lsqnonlin.py:1245-1291).
+
+    ``run(iters, lm_iters=20, tol=1e-8)``: every draw is refined by lm_iters LM
+    iterations from lambda = 5 before its cost is compared, all in one launch.
+    """
+
+    def run(self, iters: int, lm_iters: int = 20, tol=1e-8, seed: int | None = None, **kw):
+        return super().run(iters, lm_iters=lm_iters, tol=tol, seed=seed, **kw)
