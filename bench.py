@@ -269,6 +269,74 @@ def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=64, seed=77, l
     return out
 
 
+def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
+    """C3: VFA-T1 + T2* + IVIM + bi-exp T2, 1M voxels each, one persistent
+    launch (autotuned) vs one single-model launch per model."""
+    import torch
+    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline, synth
+    from pycompute_gb300.multi import MultiJob, MultiModelFitter, autotune
+    dev = torch.device("cuda")
+    ws = [synth.vfa_t1(), synth.t2star(), synth.ivim(), synth.biexp_t2()]
+    gens = []
+    for k, w in enumerate(ws):
+        true, data = pipeline.synth_gpu(w, n_per_model, seed=seed + k, device=dev)
+        gens.append((data, pipeline.init_constant(data, w.init_values)))
+    models = [(Expr(w.expr, w.pars, w.consts), w.M) for w in ws]
+
+    def make_jobs(frac=1.0):
+        jobs = []
+        for w, (data, init) in zip(ws, gens):
+            n = max(1024, int(data.shape[1] * frac))
+            jobs.append(MultiJob(init[:, :n].clone(), data[:, :n].contiguous(), w.protocol, w.lb, w.ub))
+        return jobs
+
+    t0 = time.perf_counter()
+    tuned = autotune(models, lambda: make_jobs(0.125), iters=20)
+    tune_s = time.perf_counter() - t0
+    fitter = MultiModelFitter(models, block=tuned["block"], maxrreg=tuned["maxrreg"])
+    fitter.chunk = tuned["chunk"]
+    jobs = make_jobs()
+    inits = [j.pars.clone() for j in jobs]
+
+    def run_multi():
+        for j, i0 in zip(jobs, inits):
+            j.reset(i0)
+        fitter.fit(jobs, iters)
+
+    graph = fitter.capture(jobs, iters)
+
+    def run_graph():
+        for j, i0 in zip(jobs, inits):
+            j.reset(i0)
+        graph.replay()
+
+    singles = []
+    for w, (data, init) in zip(ws, gens):
+        solm = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float32)
+        p = init.clone()
+        solm.setup(p, torch.tensor(w.protocol, device=dev), data, torch.tensor(w.lb, device=dev),
+                   torch.tensor(w.ub, device=dev))
+        singles.append((solm, p, init))
+
+    def run_singles():
+        for solm, p, init in singles:
+            p.copy_(init)
+            solm.lam_t.fill_(5.0)
+            solm.step_type_t.fill_(1)
+            solm.run(iters)
+
+    total = sum(int(d.shape[1]) for d, _ in gens)
+    ms_multi = _time_ms(run_multi)
+    ms_graph = _time_ms(run_graph)
+    ms_single = _time_ms(run_singles)
+    its = [float(j.iters.double().mean()) for j in jobs]
+    return {"workload": "mixed_vfa8_t2s16_ivim10_biexp32", "voxels": total, "iters": iters,
+            "autotuned": {k: tuned[k] for k in ("block", "maxrreg", "chunk", "ms")}, "tune_s": round(tune_s, 1),
+            "one_launch_fits_per_s": total / (ms_multi / 1e3), "graph_fits_per_s": total / (ms_graph / 1e3),
+            "per_model_launches_fits_per_s": total / (ms_single / 1e3), "mean_iters_per_model": its,
+            "ms": {"one_launch": ms_multi, "graph": ms_graph, "per_model": ms_single}}
+
+
 def run_reference_arm(args):
     ws, rank, local = _dist()
     if rank != 0:
@@ -307,14 +375,20 @@ def main():
     ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison (IVIM-16)")
     ap.add_argument("--warm-voxels", type=int, default=1 << 24)
     ap.add_argument("--only-warm", action="store_true", help="run only the warm-start comparison")
+    ap.add_argument("--only-mixed", action="store_true", help="run only the mixed-model batch comparison")
+    ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--warm-epochs", type=int, default=64)
     ap.add_argument("--warm-lam0", type=float, default=1e-3)
+    ap.add_argument("--warm-train", type=int, default=1 << 21)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.only_mixed:
+        print(json.dumps(mixed_batch_comparison()), flush=True)
+        return 0
     if args.only_warm:
         print(json.dumps(warm_start_comparison(n_eval=args.warm_voxels, epochs=args.warm_epochs,
-                                               lam0=args.warm_lam0)), flush=True)
+                                               lam0=args.warm_lam0, n_train=args.warm_train)), flush=True)
         return 0
 
     import torch
@@ -459,7 +533,12 @@ def main():
 
     warm = None
     if rank == 0 and ws == 1 and not args.no_warm:
-        warm = warm_start_comparison(n_eval=args.warm_voxels, epochs=args.warm_epochs, lam0=args.warm_lam0)
+        warm = warm_start_comparison(n_eval=args.warm_voxels, epochs=args.warm_epochs, lam0=args.warm_lam0,
+                                     n_train=args.warm_train)
+
+    mixed = None
+    if rank == 0 and ws == 1 and not args.no_mixed:
+        mixed = mixed_batch_comparison()
 
     # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
     cpu = None
@@ -499,6 +578,7 @@ def main():
             "accuracy": acc,
             "at_1e-4_vs_fp64": at_tol,
             "warm_start": warm,
+            "mixed_batch": mixed,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": clk.summary(),

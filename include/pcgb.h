@@ -180,6 +180,48 @@ int pcgb_random_search(pcgb_fitter* fitter, const void* consts, int64_t consts_s
 int pcgb_model_eval(pcgb_fitter* fitter, const void* params, const void* consts, int64_t consts_stride, void* out,
                     int64_t nprobs, const double* protocol_host, int protocol_len, void* stream);
 
+/* ---- mixed-model persistent batch (no reference counterpart) ----------------
+ *
+ * One program holds up to 8 models (each with its own protocol length); one
+ * persistent launch fits every voxel of every model: warps claim chunks of
+ * `chunk` voxels from a device work counter, so models with fast-converging
+ * voxels hand their warps to the others. Protocols and bounds are shared per
+ * model (host values in the job). The reference fits one model per program
+ * and relaunches per iteration.
+ */
+typedef struct pcgb_multi pcgb_multi;
+
+typedef struct {
+  const void* data;        /* (M, N) signals */
+  void* params;            /* (P, N) in/out */
+  void* lam;               /* (N) in/out */
+  int8_t* step_type;       /* (N) in/out */
+  void* f;                 /* (N) in/out */
+  void* first_f;           /* (N) out */
+  void* last_f;            /* (N) out */
+  int32_t* iters_done;     /* (N) in/out or NULL */
+  int64_t nprobs;          /* N */
+  const double* protocol;  /* host, C*M values */
+  const double* lb;        /* host, P values */
+  const double* ub;        /* host, P values */
+} pcgb_multi_job;
+
+/* Compile one program for n_models models (NVRTC, sm_103a, disk cache).
+ * maxrreg: register cap (0 = compiler's choice); block: threads per block. */
+int pcgb_multi_create(int n_models, const char* const* model_sources, const char* const* model_structs,
+                      const int* nparam, const int* nconst, const int* ndata, int dtype, int solve_dtype, int maxrreg,
+                      int block, const char* cache_dir, pcgb_multi** out);
+int pcgb_multi_destroy(pcgb_multi* program);
+const char* pcgb_multi_log(const pcgb_multi* program);
+/* Persistent grid size: resident blocks per SM x SMs. */
+int pcgb_multi_grid(const pcgb_multi* program);
+
+/* Fit all jobs (one per model, in program order) for `iters` iterations in one
+ * launch. work_counter: one uint32 of device scratch, zeroed by this call
+ * (cudaMemsetAsync) before the launch; grid <= 0 selects the persistent grid. */
+int pcgb_multi_run(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, int iters, double tol, double mu,
+                   double eta, double acc, double dec, int chunk, int grid, uint32_t* work_counter, void* stream);
+
 /* ---- fit pipeline (no reference counterpart) -------------------------------
  * fp32 structure-of-arrays buffers; values/lb/ub are host arrays of nparam.
  */

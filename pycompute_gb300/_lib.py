@@ -48,6 +48,13 @@ SIGNATURES = {
     "pcgb_random_search": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p,
                                    c_void_p, c_i64, c_int, c_int, c_double, c_double, c_double, c_double, c_double,
                                    ctypes.c_uint64, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
+    "pcgb_multi_create": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
+                                  c_char_p, ctypes.POINTER(c_void_p)]),
+    "pcgb_multi_destroy": (c_int, [c_void_p]),
+    "pcgb_multi_log": (c_char_p, [c_void_p]),
+    "pcgb_multi_grid": (c_int, [c_void_p]),
+    "pcgb_multi_run": (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, c_double, c_double, c_double, c_double,
+                               c_int, c_int, c_void_p, c_void_p]),
     "pcgb_model_eval": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_int, c_void_p]),
     "pcgb_pipeline_last_error": (c_char_p, []),
     "pcgb_init_constant": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p]),

@@ -574,6 +574,27 @@ __device__ void lm_grid(const PcgbLmParams& a) {
     lm_fit_voxel<Model, M, TA, TS, SHARED_C, SHARED_B>(a, a.vox_idx ? (long long)a.vox_idx[i] : i);
 }
 
+// Mixed-model persistent schedule: each warp repeatedly claims the next chunk
+// of voxels from the work counter and fits it with the chunk's model (FitJob<k>
+// is the per-model lm_fit_voxel instantiation). A warp never mixes models, so
+// models only diverge between warps; voxels of fast-converging models free
+// their warp early and it takes more work.
+template <class Dispatch>
+__device__ void multi_grid(const PcgbMultiParams& q) {
+  const int lane = threadIdx.x & 31;
+  const long long total = q.chunk_off[q.njobs];
+  for (;;) {
+    unsigned int c = 0;
+    if (lane == 0) c = atomicAdd(q.counter, 1u);
+    c = __shfl_sync(0xffffffffu, c, 0);
+    if ((long long)c >= total) break;
+    int k = 0;
+    while (k + 1 < q.njobs && (long long)c >= q.chunk_off[k + 1]) ++k;
+    const long long base = ((long long)c - q.chunk_off[k]) * q.chunk;
+    Dispatch::run(k, q.jobs[k], base, q.chunk, lane);
+  }
+}
+
 // Accumulating cost, the reference F kernel (lsqnonlin.py:157-177, 46-67):
 // f[v] += sum_i (m(p_v; c_i) - d_i)^2, voxels with step_type == 0 skipped.
 template <class Model, int M, typename TA, bool SHARED_C>

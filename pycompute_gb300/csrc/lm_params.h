@@ -5,6 +5,7 @@
 
 #define PCGB_MAX_PARAMS 8
 #define PCGB_MAX_PROTOCOL 256
+#define PCGB_MAX_MODELS 8
 
 struct PcgbLmParams {
   // structure-of-arrays, voxel index fastest; element type is the fitter's
@@ -43,4 +44,16 @@ struct PcgbLmParams {
   double shared_ub_d[PCGB_MAX_PARAMS];
   float protocol_f[PCGB_MAX_PROTOCOL];
   double protocol_d[PCGB_MAX_PROTOCOL];
+};
+
+// Launch parameters of the mixed-model persistent kernel: one job per model
+// (shared protocol and bounds), and the work queue. Chunk c (of `chunk`
+// voxels) belongs to the job k with chunk_off[k] <= c < chunk_off[k + 1];
+// warps claim chunks from *counter, which the host zeroes before the launch.
+struct PcgbMultiParams {
+  unsigned int* counter;
+  int njobs;
+  int chunk;
+  long long chunk_off[PCGB_MAX_MODELS + 1];
+  PcgbLmParams jobs[PCGB_MAX_MODELS];
 };

@@ -120,12 +120,14 @@ const std::vector<std::string>& nvrtc_options() {
   return opts;
 }
 
-int compile_cubin(const std::string& src, std::vector<char>& cubin, std::string& log) {
+int compile_cubin(const std::string& src, std::vector<char>& cubin, std::string& log,
+                  const std::vector<std::string>& extra = {}) {
   nvrtcProgram prog;
   nvrtcResult r = nvrtcCreateProgram(&prog, src.c_str(), "pcgb_fitter.cu", 0, nullptr, nullptr);
   if (r != NVRTC_SUCCESS) return fail(PCGB_ECOMPILE, "nvrtcCreateProgram: %s", nvrtcGetErrorString(r));
   std::vector<const char*> o;
   for (auto& s : nvrtc_options()) o.push_back(s.c_str());
+  for (auto& s : extra) o.push_back(s.c_str());
   r = nvrtcCompileProgram(prog, int(o.size()), o.data());
   size_t ls = 0;
   nvrtcGetProgramLogSize(prog, &ls);
@@ -232,12 +234,12 @@ int validate_create(const char* model_source, const char* model_struct, int npar
   return PCGB_OK;
 }
 
-// Compiled cubin of the program, from the disk cache when present.
-int get_cubin(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata, int dtype,
-              int solve_dtype, const char* cache_dir, std::vector<char>& cubin, std::string& log) {
-  const std::string src = program_source(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype);
+// Compiled cubin of a program source, from the disk cache when present.
+int cubin_for_source(const std::string& src, const std::vector<std::string>& extra, const char* cache_dir,
+                     std::vector<char>& cubin, std::string& log) {
   std::string key_src = src;
   for (auto& o : nvrtc_options()) key_src += "\n" + o;
+  for (auto& o : extra) key_src += "\n" + o;
   int nv_major = 0, nv_minor = 0;
   nvrtcVersion(&nv_major, &nv_minor);
   key_src += "\nnvrtc " + std::to_string(nv_major) + "." + std::to_string(nv_minor);
@@ -246,14 +248,61 @@ int get_cubin(const char* model_source, const char* model_struct, int nparam, in
   std::string cache_path;
   if (cache_dir && *cache_dir) cache_path = std::string(cache_dir) + "/pcgb_" + keyhex + ".cubin";
   if (cache_path.empty() || !read_file(cache_path, cubin)) {
-    int rc = compile_cubin(src, cubin, log);
+    int rc = compile_cubin(src, cubin, log, extra);
     if (rc) return rc;
     if (!cache_path.empty()) write_file_atomic(cache_path, cubin);
   }
   return PCGB_OK;
 }
 
+int get_cubin(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata, int dtype,
+              int solve_dtype, const char* cache_dir, std::vector<char>& cubin, std::string& log) {
+  return cubin_for_source(program_source(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype), {},
+                          cache_dir, cubin, log);
+}
+
+static_assert(sizeof(PcgbMultiParams) <= 32000, "multi-model launch parameters exceed the 32 KB kernel parameter limit");
+
+std::string multi_source(int n, const char* const* srcs, const char* const* structs, const int* P, const int* C,
+                         const int* M, int dtype, int sdtype, int block) {
+  const char* ta = dtype == PCGB_DTYPE_F64 ? "double" : "float";
+  const char* ts = sdtype == PCGB_DTYPE_F64 ? "double" : "float";
+  std::ostringstream s;
+  s << "// pcgb mixed-model program: " << n << " jobs, state=" << ta << " solve=" << ts << " block=" << block << "\n";
+  s << pcgb_embedded_lm_params_h << "\n" << pcgb_embedded_lm_kernel_cuh << "\n";
+  std::vector<std::string> seen;
+  for (int k = 0; k < n; ++k) {
+    bool dup = false;
+    for (auto& x : seen) dup = dup || x == structs[k];
+    if (!dup) {
+      s << srcs[k] << "\n";
+      seen.push_back(structs[k]);
+    }
+    s << "static_assert(" << structs[k] << "::P == " << P[k] << " && " << structs[k] << "::C == " << C[k]
+      << ", \"model shape\");\n";
+  }
+  s << "struct PcgbDispatch {\n  static __device__ __forceinline__ void run(int k, const PcgbLmParams& a, long long base,"
+       " int chunk, int lane) {\n    switch (k) {\n";
+  for (int k = 0; k < n; ++k)
+    s << "      case " << k << ":\n        for (int j = lane; j < chunk; j += 32) {\n"
+      << "          const long long v = base + j;\n          if (v < a.N) pcgb::lm_fit_voxel<" << structs[k] << ", "
+      << M[k] << ", " << ta << ", " << ts << ", true, true>(a, v);\n        }\n        break;\n";
+  s << "      default: break;\n    }\n  }\n};\n";
+  s << "extern \"C\" __global__ void __launch_bounds__(" << block
+    << ") pcgb_multi_lm(const PcgbMultiParams q) { pcgb::multi_grid<PcgbDispatch>(q); }\n";
+  return s.str();
+}
+
 }  // namespace
+
+struct pcgb_multi {
+  int n = 0, dtype = 0, block = 128, device = -1;
+  int P[PCGB_MAX_MODELS] = {}, C[PCGB_MAX_MODELS] = {}, M[PCGB_MAX_MODELS] = {};
+  cudaLibrary_t lib = nullptr;
+  cudaKernel_t kernel = nullptr;
+  int blocks_per_sm = 0, sms = 0;
+  std::string log;
+};
 
 extern "C" {
 
@@ -314,6 +363,136 @@ int pcgb_fitter_create(const char* model_source, const char* model_struct, int n
     }
   }
   *out = ft;
+  return PCGB_OK;
+}
+
+int pcgb_multi_create(int n_models, const char* const* model_sources, const char* const* model_structs,
+                      const int* nparam, const int* nconst, const int* ndata, int dtype, int solve_dtype, int maxrreg,
+                      int block, const char* cache_dir, pcgb_multi** out) {
+  g_err.clear();
+  if (!out) return fail(PCGB_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (n_models < 1 || n_models > PCGB_MAX_MODELS) return fail(PCGB_ERANGE, "1..%d models per program", PCGB_MAX_MODELS);
+  if (!model_sources || !model_structs || !nparam || !nconst || !ndata) return fail(PCGB_EINVAL, "model arrays missing");
+  if (block < 32 || block > 1024 || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to 1024");
+  if (maxrreg != 0 && (maxrreg < 32 || maxrreg > 255)) return fail(PCGB_EINVAL, "maxrreg must be 0 or 32..255");
+  for (int k = 0; k < n_models; ++k)
+    if (int rc = validate_create(model_sources[k], model_structs[k], nparam[k], nconst[k], ndata[k], dtype, solve_dtype))
+      return rc;
+  const std::string src =
+      multi_source(n_models, model_sources, model_structs, nparam, nconst, ndata, dtype, solve_dtype, block);
+  std::vector<std::string> extra;
+  if (maxrreg) extra.push_back("--maxrregcount=" + std::to_string(maxrreg));
+  std::vector<char> cubin;
+  std::string log;
+  if (int rc = cubin_for_source(src, extra, cache_dir, cubin, log)) return rc;
+  auto* m = new (std::nothrow) pcgb_multi();
+  if (!m) return fail(PCGB_ENOMEM, "out of host memory");
+  m->n = n_models;
+  m->dtype = dtype;
+  m->block = block;
+  m->log = log;
+  for (int k = 0; k < n_models; ++k) {
+    m->P[k] = nparam[k];
+    m->C[k] = nconst[k];
+    m->M[k] = ndata[k];
+  }
+  cudaError_t e = cudaGetDevice(&m->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->sms, cudaDevAttrMultiProcessorCount, m->device);
+  if (e == cudaSuccess) e = cudaLibraryLoadData(&m->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e == cudaSuccess) e = cudaLibraryGetKernel(&m->kernel, m->lib, "pcgb_multi_lm");
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m->blocks_per_sm, reinterpret_cast<const void*>(m->kernel),
+                                                      block, 0);
+  if (e != cudaSuccess) {
+    if (m->lib) cudaLibraryUnload(m->lib);
+    delete m;
+    return cuda_fail(e, "pcgb_multi_create");
+  }
+  if (m->blocks_per_sm < 1) m->blocks_per_sm = 1;
+  *out = m;
+  return PCGB_OK;
+}
+
+int pcgb_multi_destroy(pcgb_multi* m) {
+  if (!m) return PCGB_OK;
+  int rc = PCGB_OK;
+  if (m->lib) {
+    cudaError_t e = cudaLibraryUnload(m->lib);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaLibraryUnload");
+  }
+  delete m;
+  return rc;
+}
+
+const char* pcgb_multi_log(const pcgb_multi* m) { return m ? m->log.c_str() : ""; }
+
+int pcgb_multi_grid(const pcgb_multi* m) { return m ? m->blocks_per_sm * m->sms : 0; }
+
+int pcgb_multi_run(pcgb_multi* m, const pcgb_multi_job* jobs, int n_jobs, int iters, double tol, double mu,
+                   double eta, double acc, double dec, int chunk, int grid, uint32_t* work_counter, void* stream) {
+  g_err.clear();
+  if (!m) return fail(PCGB_EINVAL, "program is NULL");
+  if (!jobs || n_jobs != m->n) return fail(PCGB_EINVAL, "need one job per model of the program (%d)", m->n);
+  if (iters < 0) return fail(PCGB_EINVAL, "iters must be >= 0");
+  if (chunk < 32 || chunk % 32 || chunk > 4096) return fail(PCGB_EINVAL, "chunk must be a multiple of 32 up to 4096");
+  if (!work_counter) return fail(PCGB_EINVAL, "work_counter is NULL");
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != m->device) return fail(PCGB_EINVAL, "program was built on device %d but device %d is current", m->device, dev);
+  PcgbMultiParams q;
+  std::memset(&q, 0, sizeof(q));
+  q.counter = work_counter;
+  q.njobs = n_jobs;
+  q.chunk = chunk;
+  long long off = 0;
+  for (int k = 0; k < n_jobs; ++k) {
+    const pcgb_multi_job& j = jobs[k];
+    PcgbLmParams& a = q.jobs[k];
+    if (j.nprobs < 0) return fail(PCGB_EINVAL, "job %d: nprobs < 0", k);
+    if (j.nprobs > 0 && (!j.data || !j.params || !j.lam || !j.step_type || !j.f || !j.first_f || !j.last_f))
+      return fail(PCGB_EINVAL, "job %d: data, params, lam, step_type, f, first_f and last_f are required", k);
+    const int need = m->C[k] * m->M[k];
+    if (need > 0 && !j.protocol) return fail(PCGB_EINVAL, "job %d: protocol missing", k);
+    if (!j.lb || !j.ub) return fail(PCGB_EINVAL, "job %d: bounds missing", k);
+    for (int i = 0; i < need; ++i) {
+      a.protocol_d[i] = j.protocol[i];
+      a.protocol_f[i] = float(j.protocol[i]);
+    }
+    for (int p = 0; p < m->P[k]; ++p) {
+      a.shared_lb_d[p] = j.lb[p];
+      a.shared_ub_d[p] = j.ub[p];
+      a.shared_lb_f[p] = float(j.lb[p]);
+      a.shared_ub_f[p] = float(j.ub[p]);
+    }
+    a.pars = j.params;
+    a.data = j.data;
+    a.lam = j.lam;
+    a.step_type = reinterpret_cast<signed char*>(j.step_type);
+    a.f = j.f;
+    a.first_f = j.first_f;
+    a.last_f = j.last_f;
+    a.iters_done = j.iters_done;
+    a.N = j.nprobs;
+    a.n_items = j.nprobs;
+    a.iters = iters;
+    a.tol = tol;
+    a.mu = mu;
+    a.eta = eta;
+    a.acc = acc;
+    a.dec = dec;
+    q.chunk_off[k] = off;
+    off += (j.nprobs + chunk - 1) / chunk;
+  }
+  q.chunk_off[n_jobs] = off;
+  if (off == 0) return PCGB_OK;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), s);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  if (grid <= 0) grid = m->blocks_per_sm * m->sms;
+  void* args[] = {&q};
+  e = cudaLaunchKernel(reinterpret_cast<const void*>(m->kernel), dim3(grid), dim3(m->block), args, 0, s);
+  if (e != cudaSuccess) return cuda_fail(e, "pcgb_multi_lm");
   return PCGB_OK;
 }
 
