@@ -234,6 +234,21 @@ const char* pcgb_pipeline_last_error(void);
 int pcgb_init_constant(const float* data, int64_t n, int m, int nparam, const double* values, float* pars,
                        void* stream);
 
+/* Batched polynomial least squares, the reference's bpolyfit
+ * (pycompute/cuda/lsq.py:18-26): per voxel, the coefficients of 1, x, ..., x^deg
+ * (deg <= 3) best fitting rows [row0, row0 + rows) of y (M, n) (log y when
+ * log_y), rows <= 64. x is (rows, n) device with x_stride = n, or NULL with
+ * x_shared = rows host values. out is (deg + 1, n). FP64 Householder QR. */
+int pcgb_bpolyfit(const float* x, int64_t x_stride, const double* x_shared, const float* y, int64_t n, int row0,
+                  int rows, int deg, int log_y, float* out, void* stream);
+
+/* The IVIM notebook's segmented initialisation (test_ivim.ipynb cells 6, 10)
+ * from two degree-1 log fits (low, high: (2, n) from pcgb_bpolyfit on -b):
+ * initial parameters clipped to [lb, ub] (host, 4 values) and, when lb_out /
+ * ub_out are given, the notebook's per-voxel data-driven bounds. */
+int pcgb_ivim_segmented_init(const float* low, const float* high, int64_t n, const double* lb, const double* ub,
+                             float* pars, float* lb_out, float* ub_out, void* stream);
+
 /* Flag voxels whose fit is not trusted (non-finite cost, cost not below
  * cost_ref, or a parameter on a bound) and append their indices to idx
  * (capacity n). count (one int32 on the device) must be zero on entry and

@@ -58,6 +58,10 @@ SIGNATURES = {
     "pcgb_model_eval": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_int, c_void_p]),
     "pcgb_pipeline_last_error": (c_char_p, []),
     "pcgb_init_constant": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p]),
+    "pcgb_bpolyfit": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_i64, c_int, c_int, c_int, c_int, c_void_p,
+                              c_void_p]),
+    "pcgb_ivim_segmented_init": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                         c_void_p]),
     "pcgb_fallback_flags": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_int, c_void_p, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_void_p]),
     "pcgb_fallback_prepare": (c_int, [c_void_p, c_i64, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p, c_void_p,
@@ -111,7 +115,7 @@ def check(fn_name: str, rc: int):
         L = lib()
         if fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")):
             err = L.pcgb_mlp_last_error
-        elif fn_name.startswith(("pcgb_init_constant", "pcgb_fallback")):
+        elif fn_name.startswith(("pcgb_init_constant", "pcgb_fallback", "pcgb_bpolyfit", "pcgb_ivim")):
             err = L.pcgb_pipeline_last_error
         else:
             err = L.pcgb_last_error

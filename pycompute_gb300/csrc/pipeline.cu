@@ -128,6 +128,113 @@ __global__ void fallback_select_kernel(const int* idx, long long n_items, long l
   if (which) which[v] = refit ? 1 : 0;
 }
 
+// ---- segmented log-linear initialisation --------------------------------------
+
+constexpr int kMaxFitRows = 64;
+constexpr int kMaxDeg = 3;
+
+struct PolyArgs {
+  const float* x;        // (rows, n) per voxel, or null: shared xs[]
+  long long xstride;     // n, or 0 with shared x
+  float xs[kMaxFitRows];
+  const float* y;        // (M, n); rows [r0, r0 + rows) are fitted
+  long long n;
+  int r0, rows, deg, log_y;
+  float* out;            // (deg + 1, n): coefficients of x^0 .. x^deg
+};
+
+// Per-voxel least squares of y (or log y) on 1, x, ..., x^deg: the batched
+// pinv(A) @ y of the reference's bpolyfit (pycompute/cuda/lsq.py:18-26). For
+// a full-rank design this is the least-squares solution, computed here by
+// Householder QR in FP64 (rows <= 64, deg <= 3); a rank-deficient column gets
+// coefficient 0.
+__global__ void bpolyfit_kernel(const PolyArgs a) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.n) return;
+  const int m = a.rows, q = a.deg + 1;
+  double A[kMaxFitRows][kMaxDeg + 1];
+  double b[kMaxFitRows];
+  for (int i = 0; i < m; ++i) {
+    const double xi = a.x ? double(a.x[(long long)i * a.xstride + v]) : double(a.xs[i]);
+    double pw = 1.0;
+    for (int j = 0; j < q; ++j) {
+      A[i][j] = pw;
+      pw *= xi;
+    }
+    const double yi = double(a.y[(long long)(a.r0 + i) * a.n + v]);
+    b[i] = a.log_y ? log(yi) : yi;
+  }
+  double R[kMaxDeg + 1];
+  for (int j = 0; j < q; ++j) {
+    double nrm = 0.0;
+    for (int i = j; i < m; ++i) nrm += A[i][j] * A[i][j];
+    nrm = sqrt(nrm);
+    if (!(nrm > 0.0)) {
+      R[j] = 0.0;
+      continue;
+    }
+    const double alpha = A[j][j] > 0 ? -nrm : nrm;
+    A[j][j] -= alpha;  // v = x - alpha e1, stored in column j
+    double vv = 0.0;
+    for (int i = j; i < m; ++i) vv += A[i][j] * A[i][j];
+    for (int k = j + 1; k < q; ++k) {
+      double s = 0.0;
+      for (int i = j; i < m; ++i) s += A[i][j] * A[i][k];
+      s = 2.0 * s / vv;
+      for (int i = j; i < m; ++i) A[i][k] -= s * A[i][j];
+    }
+    double s = 0.0;
+    for (int i = j; i < m; ++i) s += A[i][j] * b[i];
+    s = 2.0 * s / vv;
+    for (int i = j; i < m; ++i) b[i] -= s * A[i][j];
+    R[j] = alpha;
+  }
+  double c[kMaxDeg + 1];
+  for (int j = q - 1; j >= 0; --j) {
+    double t = b[j];
+    for (int k = j + 1; k < q; ++k) t -= A[j][k] * c[k];
+    c[j] = fabs(R[j]) > 1e-300 ? t / R[j] : 0.0;
+  }
+  for (int j = 0; j < q; ++j) a.out[(long long)j * a.n + v] = float(c[j]);
+}
+
+struct IvimInitArgs {
+  const float* low;    // (2, n): log-intercept and slope of the low-b fit
+  const float* high;   // (2, n): the same for the high-b fit
+  long long n;
+  float lb0[4], ub0[4];
+  float* pars;         // (4, n) out
+  float* lb;           // (4, n) out, data-driven bounds
+  float* ub;           // (4, n) out
+};
+
+__device__ __forceinline__ float finite_or_zero(float x) { return isfinite(x) ? x : 0.f; }
+
+// The IVIM notebook's segmented initialisation (test_ivim.ipynb cells 6 and
+// 10): S0 = exp(low intercept), f = 1 - exp(high intercept) / S0,
+// D* = low slope, D = high slope (non-finite -> 0, then clipped to the fixed
+// bounds), and per-voxel bounds S0/2..2 S0 (within 500..20000), f +- 0.4
+// (within 0.001..0.999), D*/200..200 D* (within 1e-6..0.1), D/200..200 D
+// (within 1e-8..0.02).
+__global__ void ivim_segmented_init_kernel(const IvimInitArgs a) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v >= a.n) return;
+  const float s0 = expf(a.low[v]);
+  const float s1 = expf(a.high[v]);
+  float p[4] = {finite_or_zero(s0), finite_or_zero(1.f - s1 / s0), finite_or_zero(a.low[a.n + v]),
+                finite_or_zero(a.high[a.n + v])};
+  for (int k = 0; k < 4; ++k) p[k] = fminf(fmaxf(p[k], a.lb0[k]), a.ub0[k]);
+  const float lo[4] = {fmaxf(p[0] / 2.f, 500.f), fmaxf(p[1] - 0.4f, 0.001f), fmaxf(p[2] / 200.f, 1e-6f),
+                       fmaxf(p[3] / 200.f, 1e-8f)};
+  const float hi[4] = {fminf(p[0] * 2.f, 20000.f), fminf(p[1] + 0.4f, 0.999f), fminf(p[2] * 200.f, 0.1f),
+                       fminf(p[3] * 200.f, 0.02f)};
+  for (int k = 0; k < 4; ++k) {
+    a.pars[(long long)k * a.n + v] = p[k];
+    if (a.lb) a.lb[(long long)k * a.n + v] = lo[k];
+    if (a.ub) a.ub[(long long)k * a.n + v] = hi[k];
+  }
+}
+
 unsigned blocks(long long n) { return unsigned((n + 255) / 256 > 0 ? (n + 255) / 256 : 1); }
 
 }  // namespace pcgb_pipe
@@ -206,6 +313,47 @@ int pcgb_fallback_prepare(const int32_t* idx, int64_t n_items, int64_t n, int np
   a.step_type = reinterpret_cast<signed char*>(step_type);
   a.f = f;
   fallback_prepare_kernel<<<blocks(n_items), 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  return cuda_rc();
+}
+
+int pcgb_bpolyfit(const float* x, int64_t x_stride, const double* x_shared, const float* y, int64_t n, int row0,
+                  int rows, int deg, int log_y, float* out, void* stream) {
+  if (n < 0 || rows < 1 || rows > kMaxFitRows || deg < 0 || deg > kMaxDeg || row0 < 0 || !y || !out)
+    return fail(PCGB_EINVAL, "bpolyfit: rows 1..64, deg 0..3, y and out required");
+  if (!x && !x_shared) return fail(PCGB_EINVAL, "bpolyfit: x or x_shared required");
+  if (n == 0) return PCGB_OK;
+  PolyArgs a{};
+  a.x = x;
+  a.xstride = x ? x_stride : 0;
+  if (!x)
+    for (int i = 0; i < rows; ++i) a.xs[i] = float(x_shared[i]);
+  a.y = y;
+  a.n = n;
+  a.r0 = row0;
+  a.rows = rows;
+  a.deg = deg;
+  a.log_y = log_y;
+  a.out = out;
+  bpolyfit_kernel<<<blocks(n), 128, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  return cuda_rc();
+}
+
+int pcgb_ivim_segmented_init(const float* low, const float* high, int64_t n, const double* lb, const double* ub,
+                             float* pars, float* lb_out, float* ub_out, void* stream) {
+  if (n < 0 || !low || !high || !lb || !ub || !pars) return fail(PCGB_EINVAL, "ivim_segmented_init: bad arguments");
+  if (n == 0) return PCGB_OK;
+  IvimInitArgs a{};
+  a.low = low;
+  a.high = high;
+  a.n = n;
+  for (int k = 0; k < 4; ++k) {
+    a.lb0[k] = float(lb[k]);
+    a.ub0[k] = float(ub[k]);
+  }
+  a.pars = pars;
+  a.lb = lb_out;
+  a.ub = ub_out;
+  ivim_segmented_init_kernel<<<blocks(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
   return cuda_rc();
 }
 

@@ -161,3 +161,43 @@ class WarmStartFitter:
             for (n0, e0), (n1, e1) in zip(ev[:-1], ev[1:]):
                 timings[n1] = timings.get(n1, 0.0) + e0.elapsed_time(e1)
         return dict(pars=pars, cost=cost, n_fallback=nfb, n_refit_kept=kept_refit, step_type=solm.step_type_t)
+
+
+def bpolyfit(y: torch.Tensor, deg: int, x_shared=None, x: torch.Tensor | None = None, row0: int = 0,
+             rows: int | None = None, log_y: bool = False) -> torch.Tensor:
+    """Per-voxel polynomial least squares (the reference's bpolyfit, pycompute/cuda/lsq.py:18-26).
+
+    Fits rows [row0, row0 + rows) of y (M, N) (or their log) on 1, x, ..., x^deg;
+    x is a shared host sequence of `rows` values or a (rows, N) device tensor.
+    Returns the (deg + 1, N) coefficients.
+    """
+    M, N = y.shape
+    rows = M - row0 if rows is None else rows
+    out = torch.empty((deg + 1, N), dtype=torch.float32, device=y.device)
+    xs = _dvec(x_shared) if x_shared is not None else None
+    rc = _lib.lib().pcgb_bpolyfit(_p(x), N if x is not None else 0, xs, _p(y), N, int(row0), int(rows), int(deg),
+                                  int(log_y), _p(out), _stream())
+    _lib.check("pcgb_bpolyfit", rc)
+    return out
+
+
+def ivim_segmented_init(data: torch.Tensor, bvals, low: tuple[int, int], high: tuple[int, int], lb, ub,
+                        bounds: bool = True):
+    """The IVIM notebook's initialisation (test_ivim.ipynb cells 6 and 10).
+
+    Degree-1 fits of log S against -b on rows [low[0], low[1]) and
+    [high[0], high[1]) give S0, f, D* and D; with ``bounds`` also the per-voxel
+    data-driven bounds of the notebook. Returns (pars, lb, ub) as (4, N).
+    """
+    b = [float(v) for v in bvals]
+    N = data.shape[1]
+    lo = bpolyfit(data, 1, x_shared=[-v for v in b[low[0]:low[1]]], row0=low[0], rows=low[1] - low[0], log_y=True)
+    hi = bpolyfit(data, 1, x_shared=[-v for v in b[high[0]:high[1]]], row0=high[0], rows=high[1] - high[0],
+                  log_y=True)
+    pars = torch.empty((4, N), dtype=torch.float32, device=data.device)
+    lbo = torch.empty_like(pars) if bounds else None
+    ubo = torch.empty_like(pars) if bounds else None
+    rc = _lib.lib().pcgb_ivim_segmented_init(_p(lo), _p(hi), N, _dvec(lb), _dvec(ub), _p(pars), _p(lbo), _p(ubo),
+                                             _stream())
+    _lib.check("pcgb_ivim_segmented_init", rc)
+    return pars, lbo, ubo

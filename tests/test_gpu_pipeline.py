@@ -103,3 +103,26 @@ def test_trained_network_beats_plain_lm_at_equal_iterations():
     # the network start is worth several LM iterations
     assert e_warm < 0.1 * e_plain, (e_warm, e_plain)
     assert res["n_fallback"] < 0.2 * data.shape[1]
+
+
+def test_bpolyfit_and_ivim_segmented_init_match_oracle():
+    from oracle import lsq_oracle
+    w = synth.ivim(synth.IVIM_B21, name="ivim21")
+    true, data = pipeline.synth_gpu(w, 20000, seed=4, device=DEV)
+    d = data.cpu().numpy()
+    b = np.array(w.protocol)
+    for deg in (1, 2, 3):
+        got = pipeline.bpolyfit(data, deg, x_shared=list(-b[2:14] / 1000.0), row0=2, rows=12, log_y=True)
+        want = lsq_oracle.bpolyfit(-b[2:14] / 1000.0, np.log(d[2:14]), deg)
+        np.testing.assert_allclose(got.cpu().numpy(), want, rtol=2e-5, atol=2e-5 * np.abs(want).max())
+    # per-voxel x
+    xv = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(-b[:10, None], (10, 20000)).astype(np.float32)))
+    got = pipeline.bpolyfit(data, 1, x=xv.to(DEV), rows=10, log_y=True)
+    want = lsq_oracle.bpolyfit(-b[:10], np.log(d[:10]), 1)
+    np.testing.assert_allclose(got.cpu().numpy(), want, rtol=2e-5, atol=1e-7)
+    # the notebook recipe on 21 b-values: rows [0, 10) and [15, 21)
+    pars, lbv, ubv = pipeline.ivim_segmented_init(data, w.protocol, (0, 10), (15, 21), w.lb, w.ub)
+    p_o, lb_o, ub_o = lsq_oracle.ivim_segmented_init(d, w.protocol, slice(0, 10), slice(15, 21), w.lb, w.ub)
+    np.testing.assert_allclose(pars.cpu().numpy(), p_o, rtol=1e-4, atol=1e-6)
+    np.testing.assert_allclose(lbv.cpu().numpy(), lb_o, rtol=1e-4, atol=1e-8)
+    np.testing.assert_allclose(ubv.cpu().numpy(), ub_o, rtol=1e-4, atol=1e-8)
