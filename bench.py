@@ -295,6 +295,7 @@ def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
     tune_s = time.perf_counter() - t0
     fitter = MultiModelFitter(models, block=tuned["block"], maxrreg=tuned["maxrreg"])
     fitter.chunk = tuned["chunk"]
+    fitter.order = tuned.get("order")
     jobs = make_jobs()
     inits = [j.pars.clone() for j in jobs]
 
@@ -331,7 +332,8 @@ def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
     ms_single = _time_ms(run_singles)
     its = [float(j.iters.double().mean()) for j in jobs]
     return {"workload": "mixed_vfa8_t2s16_ivim10_biexp32", "voxels": total, "iters": iters,
-            "autotuned": {k: tuned[k] for k in ("block", "maxrreg", "chunk", "ms")}, "tune_s": round(tune_s, 1),
+            "autotuned": {k: tuned.get(k) for k in ("block", "maxrreg", "chunk", "order", "ms")},
+            "tune_s": round(tune_s, 1),
             "one_launch_fits_per_s": total / (ms_multi / 1e3), "graph_fits_per_s": total / (ms_graph / 1e3),
             "per_model_launches_fits_per_s": total / (ms_single / 1e3), "mean_iters_per_model": its,
             "ms": {"one_launch": ms_multi, "graph": ms_graph, "per_model": ms_single}}

@@ -217,10 +217,13 @@ const char* pcgb_multi_log(const pcgb_multi* program);
 int pcgb_multi_grid(const pcgb_multi* program);
 
 /* Fit all jobs (one per model, in program order) for `iters` iterations in one
- * launch. work_counter: one uint32 of device scratch, zeroed by this call
+ * launch. order (host, may be NULL = program order) is the order in which the
+ * work queue hands out the jobs' chunks (longest work first shortens the
+ * tail). work_counter: one uint32 of device scratch, zeroed by this call
  * (cudaMemsetAsync) before the launch; grid <= 0 selects the persistent grid. */
-int pcgb_multi_run(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, int iters, double tol, double mu,
-                   double eta, double acc, double dec, int chunk, int grid, uint32_t* work_counter, void* stream);
+int pcgb_multi_run(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, const int* order, int iters,
+                   double tol, double mu, double eta, double acc, double dec, int chunk, int grid,
+                   uint32_t* work_counter, void* stream);
 
 /* ---- fit pipeline (no reference counterpart) -------------------------------
  * fp32 structure-of-arrays buffers; values/lb/ub are host arrays of nparam.
@@ -311,21 +314,23 @@ int pcgb_mlp_mse_grad(const float* y, const float* t, int64_t ldy, int64_t batch
 int pcgb_adam_step(float* master, float* m, float* v, float* grad, void* w_bf16, int64_t rows, int64_t ld,
                    int64_t rows_live, float lr, float b1, float b2, float eps, const float* corr, void* stream);
 
-/* Training inputs x_rows (n x ldx) bf16 = signals / max per voxel, column nin
- * = 1; snorm[v] = that maximum. With params/targets, also the normalised
+/* Training inputs x_rows (n x ldx) bf16 = signals / max per voxel (or
+ * log(max(signals / max, 1e-6)) with log_in), column nin = 1; snorm[v] = that
+ * maximum. With params/targets, also the normalised
  * targets (n x ldt): kind 0 p/snorm, 1 p, 2 log p, then (g - mean) / std.
  * signals (nin, n) and params (nout, n) are structure-of-arrays; kinds, mean,
  * stdv are device arrays of nout entries. */
-int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, void* x_rows, int64_t ldx, float* snorm,
+int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, int log_in, void* x_rows, int64_t ldx, float* snorm,
                      const float* params, int nout, const int* kinds, const float* mean, const float* stdv,
                      float* targets, int64_t ldt, void* stream);
 
 /* Fused inference of all four layers: signals (nin, n) -> initial parameters
- * out (nout, n), clamped to [lb, ub]. w_bf16 / w_master are host arrays of the
+ * out (nout, n), clamped to [lb, ub]; log_in selects the input transform the
+ * network was trained with. w_bf16 / w_master are host arrays of the
  * four layers' device pointers; kinds, mean, stdv, lb, ub are host arrays of
  * nout entries. nin must be 16. */
-int pcgb_mlp_forward(const float* signals, int64_t n, int nin, const void* const* w_bf16, const float* const* w_master,
-                     int nout, const int* kinds, const float* mean, const float* stdv, const float* lb,
+int pcgb_mlp_forward(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
+                     const float* const* w_master, int nout, const int* kinds, const float* mean, const float* stdv, const float* lb,
                      const float* ub, float* out, void* stream);
 
 #ifdef __cplusplus

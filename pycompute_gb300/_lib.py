@@ -53,8 +53,8 @@ SIGNATURES = {
     "pcgb_multi_destroy": (c_int, [c_void_p]),
     "pcgb_multi_log": (c_char_p, [c_void_p]),
     "pcgb_multi_grid": (c_int, [c_void_p]),
-    "pcgb_multi_run": (c_int, [c_void_p, c_void_p, c_int, c_int, c_double, c_double, c_double, c_double, c_double,
-                               c_int, c_int, c_void_p, c_void_p]),
+    "pcgb_multi_run": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_double, c_double, c_double, c_double,
+                               c_double, c_int, c_int, c_void_p, c_void_p]),
     "pcgb_model_eval": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_int, c_void_p]),
     "pcgb_pipeline_last_error": (c_char_p, []),
     "pcgb_init_constant": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p]),
@@ -75,10 +75,10 @@ SIGNATURES = {
                                   c_void_p]),
     "pcgb_adam_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_i64, c_i64, ctypes.c_float,
                                ctypes.c_float, ctypes.c_float, ctypes.c_float, c_void_p, c_void_p]),
-    "pcgb_mlp_prepare": (c_int, [c_void_p, c_i64, c_int, c_void_p, c_i64, c_void_p, c_void_p, c_int, c_void_p,
+    "pcgb_mlp_prepare": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_i64, c_void_p, c_void_p, c_int, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
-    "pcgb_mlp_forward": (c_int, [c_void_p, c_i64, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
-                                 c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pcgb_mlp_forward": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+                                 c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 

@@ -588,9 +588,10 @@ __device__ void multi_grid(const PcgbMultiParams& q) {
     if (lane == 0) c = atomicAdd(q.counter, 1u);
     c = __shfl_sync(0xffffffffu, c, 0);
     if ((long long)c >= total) break;
-    int k = 0;
-    while (k + 1 < q.njobs && (long long)c >= q.chunk_off[k + 1]) ++k;
-    const long long base = ((long long)c - q.chunk_off[k]) * q.chunk;
+    int t = 0;
+    while (t + 1 < q.njobs && (long long)c >= q.chunk_off[t + 1]) ++t;
+    const int k = q.order[t];
+    const long long base = ((long long)c - q.chunk_off[t]) * q.chunk;
     Dispatch::run(k, q.jobs[k], base, q.chunk, lane);
   }
 }

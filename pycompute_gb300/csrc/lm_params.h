@@ -47,13 +47,15 @@ struct PcgbLmParams {
 };
 
 // Launch parameters of the mixed-model persistent kernel: one job per model
-// (shared protocol and bounds), and the work queue. Chunk c (of `chunk`
-// voxels) belongs to the job k with chunk_off[k] <= c < chunk_off[k + 1];
-// warps claim chunks from *counter, which the host zeroes before the launch.
+// (shared protocol and bounds), and the work queue. The queue lists the jobs
+// in the order order[0..njobs-1]; chunk c (of `chunk` voxels) belongs to job
+// order[t] with chunk_off[t] <= c < chunk_off[t + 1]; warps claim chunks from
+// *counter, which the host zeroes before the launch.
 struct PcgbMultiParams {
   unsigned int* counter;
   int njobs;
   int chunk;
+  int order[PCGB_MAX_MODELS];
   long long chunk_off[PCGB_MAX_MODELS + 1];
   PcgbLmParams jobs[PCGB_MAX_MODELS];
 };

@@ -257,10 +257,16 @@ __global__ void adam_kernel(float* master, float* m, float* v, float* grad, bf16
 
 // ---- training inputs and targets --------------------------------------------
 
-// x_rows (n x ldx) bf16 = signals / max(signals) per voxel, column nin = 1,
-// remaining padding 0; snorm[v] = the divisor. signals are SoA (nin, n).
+// Network input of one sample: s / max, or log(max(s / max, 1e-6)) with log_in.
+__device__ __forceinline__ float input_transform(float s, float inv, int log_in) {
+  const float x = s * inv;
+  return log_in ? logf(fmaxf(x, 1e-6f)) : x;
+}
+
+// x_rows (n x ldx) bf16 = transformed signals per voxel, column nin = 1,
+// remaining padding 0; snorm[v] = the per-voxel maximum. signals are SoA (nin, n).
 __global__ void prepare_inputs_kernel(const float* signals, long long n, int nin, bf16* x_rows, long long ldx,
-                                      float* snorm) {
+                                      float* snorm, int log_in) {
   const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (v >= n) return;
   float mx = 0.f;
@@ -268,7 +274,7 @@ __global__ void prepare_inputs_kernel(const float* signals, long long n, int nin
   mx = fmaxf(mx, 1e-20f);
   const float inv = 1.f / mx;
   for (int k = 0; k < ldx; ++k) {
-    float x = k < nin ? signals[(long long)k * n + v] * inv : (k == nin ? 1.f : 0.f);
+    float x = k < nin ? input_transform(signals[(long long)k * n + v], inv, log_in) : (k == nin ? 1.f : 0.f);
     x_rows[v * ldx + k] = __float2bfloat16_rn(x);
   }
   if (snorm) snorm[v] = mx;
@@ -305,6 +311,7 @@ struct InferArgs {
   const bf16* w[4];      // layer weights (rows x ld), ld = in + 8
   const float* mw[4];    // fp32 master copies; column `in` = bias
   int nout;
+  int log_in;
   int kinds[NOUT_PAD];
   float mean[NOUT_PAD], stdv[NOUT_PAD], lb[NOUT_PAD], ub[NOUT_PAD];
   float* out;            // SoA (nout, n)
@@ -412,10 +419,11 @@ __global__ void __launch_bounds__(256) mlp_infer_kernel(const InferArgs p) {
 #pragma unroll
     for (int kt = 0; kt < KT1; ++kt) {
       uint32_t a[4];
-      a[0] = pack_bf16(x0[kt][0] * i0, x0[kt][1] * i0);
-      a[1] = pack_bf16(x1[kt][0] * i1, x1[kt][1] * i1);
-      a[2] = pack_bf16(x0[kt][2] * i0, x0[kt][3] * i0);
-      a[3] = pack_bf16(x1[kt][2] * i1, x1[kt][3] * i1);
+      const int li = p.log_in;
+      a[0] = pack_bf16(input_transform(x0[kt][0], i0, li), input_transform(x0[kt][1], i0, li));
+      a[1] = pack_bf16(input_transform(x1[kt][0], i1, li), input_transform(x1[kt][1], i1, li));
+      a[2] = pack_bf16(input_transform(x0[kt][2], i0, li), input_transform(x0[kt][3], i0, li));
+      a[3] = pack_bf16(input_transform(x1[kt][2], i1, li), input_transform(x1[kt][3], i1, li));
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         uint32_t b[4];
@@ -530,14 +538,14 @@ int pcgb_adam_step(float* master, float* m, float* v, float* grad, void* w_bf16,
   return e == cudaSuccess ? PCGB_OK : mlp_fail(PCGB_ECUDA, cudaGetErrorString(e));
 }
 
-int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, void* x_rows, int64_t ldx, float* snorm,
+int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, int log_in, void* x_rows, int64_t ldx, float* snorm,
                      const float* params, int nout, const int* kinds, const float* mean, const float* stdv,
                      float* targets, int64_t ldt, void* stream) {
   if (n < 0 || nin <= 0 || ldx < nin + 1) return mlp_fail(PCGB_EINVAL, "bad prepare sizes");
   if (n == 0) return PCGB_OK;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   prepare_inputs_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(signals, n, nin, static_cast<bf16*>(x_rows), ldx,
-                                                                   snorm);
+                                                                   snorm, log_in);
   if (params && targets) {
     if (nout <= 0 || ldt < nout) return mlp_fail(PCGB_EINVAL, "bad target sizes");
     prepare_targets_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(params, snorm, n, nout, kinds, mean, stdv,
@@ -547,8 +555,8 @@ int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, void* x_rows, int
   return e == cudaSuccess ? PCGB_OK : mlp_fail(PCGB_ECUDA, cudaGetErrorString(e));
 }
 
-int pcgb_mlp_forward(const float* signals, int64_t n, int nin, const void* const* w_bf16, const float* const* w_master,
-                     int nout, const int* kinds, const float* mean, const float* stdv, const float* lb,
+int pcgb_mlp_forward(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
+                     const float* const* w_master, int nout, const int* kinds, const float* mean, const float* stdv, const float* lb,
                      const float* ub, float* out, void* stream) {
   if (n < 0) return mlp_fail(PCGB_EINVAL, "n must be >= 0");
   if (nin != 16) return mlp_fail(PCGB_EINVAL, "the fused forward is built for 16 inputs");
@@ -562,6 +570,7 @@ int pcgb_mlp_forward(const float* signals, int64_t n, int nin, const void* const
     a.mw[l] = w_master[l];
   }
   a.nout = nout;
+  a.log_in = log_in;
   for (int k = 0; k < NOUT_PAD; ++k) {
     a.kinds[k] = k < nout ? kinds[k] : 1;
     a.mean[k] = k < nout ? mean[k] : 0.f;

@@ -429,8 +429,9 @@ const char* pcgb_multi_log(const pcgb_multi* m) { return m ? m->log.c_str() : ""
 
 int pcgb_multi_grid(const pcgb_multi* m) { return m ? m->blocks_per_sm * m->sms : 0; }
 
-int pcgb_multi_run(pcgb_multi* m, const pcgb_multi_job* jobs, int n_jobs, int iters, double tol, double mu,
-                   double eta, double acc, double dec, int chunk, int grid, uint32_t* work_counter, void* stream) {
+int pcgb_multi_run(pcgb_multi* m, const pcgb_multi_job* jobs, int n_jobs, const int* order, int iters, double tol,
+                   double mu, double eta, double acc, double dec, int chunk, int grid, uint32_t* work_counter,
+                   void* stream) {
   g_err.clear();
   if (!m) return fail(PCGB_EINVAL, "program is NULL");
   if (!jobs || n_jobs != m->n) return fail(PCGB_EINVAL, "need one job per model of the program (%d)", m->n);
@@ -445,7 +446,13 @@ int pcgb_multi_run(pcgb_multi* m, const pcgb_multi_job* jobs, int n_jobs, int it
   q.counter = work_counter;
   q.njobs = n_jobs;
   q.chunk = chunk;
-  long long off = 0;
+  bool used[PCGB_MAX_MODELS] = {};
+  for (int t = 0; t < n_jobs; ++t) {
+    const int k = order ? order[t] : t;
+    if (k < 0 || k >= n_jobs || used[k]) return fail(PCGB_EINVAL, "order must be a permutation of 0..n_jobs-1");
+    used[k] = true;
+    q.order[t] = k;
+  }
   for (int k = 0; k < n_jobs; ++k) {
     const pcgb_multi_job& j = jobs[k];
     PcgbLmParams& a = q.jobs[k];
@@ -481,8 +488,11 @@ int pcgb_multi_run(pcgb_multi* m, const pcgb_multi_job* jobs, int n_jobs, int it
     a.eta = eta;
     a.acc = acc;
     a.dec = dec;
-    q.chunk_off[k] = off;
-    off += (j.nprobs + chunk - 1) / chunk;
+  }
+  long long off = 0;
+  for (int t = 0; t < n_jobs; ++t) {
+    q.chunk_off[t] = off;
+    off += (jobs[q.order[t]].nprobs + chunk - 1) / chunk;
   }
   q.chunk_off[n_jobs] = off;
   if (off == 0) return PCGB_OK;

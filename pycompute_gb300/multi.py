@@ -87,6 +87,7 @@ class MultiModelFitter:
         self._counter = None
         self.chunk = 64
         self.grid = 0
+        self.order = None  # queue order of the jobs (None = program order)
 
     def key(self) -> str:
         h = hashlib.sha1()
@@ -121,13 +122,20 @@ class MultiModelFitter:
     def persistent_grid(self) -> int:
         return _lib.lib().pcgb_multi_grid(self.build())
 
+    def heaviest_first(self) -> list[int]:
+        """Queue order by decreasing work per iteration (samples x parameters^2)."""
+        cost = [nd * gm.P * gm.P for gm, nd in self.models]
+        return sorted(range(len(cost)), key=lambda k: -cost[k])
+
     def fit(self, jobs: list[MultiJob], iters: int, tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0,
-            chunk: int | None = None, grid: int | None = None):
+            chunk: int | None = None, grid: int | None = None, order: list[int] | None = None):
         if len(jobs) != len(self.models):
             raise ValueError("one job per model")
         prog = self.build()
         arr = (_Job * len(jobs))(*[j.ctype() for j in jobs])
-        rc = _lib.lib().pcgb_multi_run(prog, arr, len(jobs), int(iters), float(tol), float(mu), float(eta),
+        order = self.order if order is None else order
+        ordc = (ctypes.c_int * len(jobs))(*order) if order is not None else None
+        rc = _lib.lib().pcgb_multi_run(prog, arr, len(jobs), ordc, int(iters), float(tol), float(mu), float(eta),
                                        float(acc), float(dec), int(chunk or self.chunk),
                                        int(self.grid if grid is None else grid),
                                        ctypes.c_void_p(self._counter.data_ptr()), ctypes.c_void_p(_stream_ptr()))
@@ -184,18 +192,20 @@ def autotune(models: list, make_jobs, iters: int, dtype=torch.float32, solve_dty
             except _lib.PcgbError:
                 continue
             for chunk in chunks:
-                times = []
-                for r in range(reps + 1):
-                    for j, i0 in zip(jobs, inits):
-                        j.reset(i0)
-                    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                    s.record()
-                    fitter.fit(jobs, iters, chunk=chunk)
-                    e.record()
-                    torch.cuda.synchronize()
-                    if r:
-                        times.append(s.elapsed_time(e))
-                results.append({"block": block, "maxrreg": maxrreg, "chunk": chunk, "ms": min(times)})
+                for order in (list(range(len(models))), fitter.heaviest_first()):
+                    times = []
+                    for r in range(reps + 1):
+                        for j, i0 in zip(jobs, inits):
+                            j.reset(i0)
+                        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                        s.record()
+                        fitter.fit(jobs, iters, chunk=chunk, order=order)
+                        e.record()
+                        torch.cuda.synchronize()
+                        if r:
+                            times.append(s.elapsed_time(e))
+                    results.append({"block": block, "maxrreg": maxrreg, "chunk": chunk, "order": order,
+                                    "ms": min(times)})
     best = min(results, key=lambda r: r["ms"])
     out = dict(best, gpu=gpu, trials=results, tune_s=round(time.perf_counter() - t0, 2))
     cache[key] = out

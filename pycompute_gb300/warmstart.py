@@ -8,7 +8,9 @@ epilogues and split-K weight gradients, a mean-squared-error gradient, Adam,
 and a fused four-layer inference kernel. One training step (forward, backward,
 Adam on all layers) is captured once as a CUDA graph and replayed per batch.
 
-Inputs are the signals divided by their per-voxel maximum. Targets are the
+Inputs are the signals divided by their per-voxel maximum, or (``log_in``,
+the default) the logarithm of that ratio, which turns exponential decays into
+near-linear curves. Targets are the
 parameters in a normalised space chosen per output ("kinds"): 0 = value
 divided by the signal maximum (an amplitude such as S0), 1 = the value itself
 (a fraction such as f), 2 = its logarithm (a rate or diffusivity), each then
@@ -58,12 +60,13 @@ class _Layer:
 class WarmStartMLP:
     """Signal curve -> LM initial parameters (see module docstring)."""
 
-    def __init__(self, nin: int, nout: int, kinds, lb, ub, device=None, seed: int = 0):
+    def __init__(self, nin: int, nout: int, kinds, lb, ub, device=None, seed: int = 0, log_in: bool = True):
         if nin != 16:
             raise ValueError("the fused inference kernel is built for 16 inputs")
         if not 1 <= nout <= 8:
             raise ValueError("nout must be 1..8")
         self.nin, self.nout = nin, nout
+        self.log_in = bool(log_in)
         self.kinds = list(kinds)
         self.lb = [float(x) for x in lb]
         self.ub = [float(x) for x in ub]
@@ -89,7 +92,8 @@ class WarmStartMLP:
 
     # ---- persistence -----------------------------------------------------
     def state_dict(self) -> dict:
-        d = {"nin": self.nin, "nout": self.nout, "kinds": np.array(self.kinds), "lb": np.array(self.lb),
+        d = {"nin": self.nin, "nout": self.nout, "log_in": int(self.log_in), "kinds": np.array(self.kinds),
+             "lb": np.array(self.lb),
              "ub": np.array(self.ub), "mean": self.mean, "std": self.std, "step": self.step}
         for i, L in enumerate(self.layers):
             d[f"w{i}"] = L.master.cpu().numpy()
@@ -101,7 +105,8 @@ class WarmStartMLP:
     @classmethod
     def load(cls, path: str, device=None) -> "WarmStartMLP":
         z = np.load(path)
-        net = cls(int(z["nin"]), int(z["nout"]), list(z["kinds"]), list(z["lb"]), list(z["ub"]), device)
+        net = cls(int(z["nin"]), int(z["nout"]), list(z["kinds"]), list(z["lb"]), list(z["ub"]), device,
+                  log_in=bool(int(z["log_in"])) if "log_in" in z.files else False)
         net.mean, net.std, net.step = z["mean"].astype(np.float32), z["std"].astype(np.float32), int(z["step"])
         for i, L in enumerate(net.layers):
             L.master.copy_(torch.from_numpy(z[f"w{i}"]))
@@ -120,7 +125,8 @@ class WarmStartMLP:
             kinds = torch.tensor(self.kinds, dtype=torch.int32, device=self.device)
             mean = torch.from_numpy(self.mean).to(self.device)
             std = torch.from_numpy(self.std).to(self.device)
-        rc = _lib.lib().pcgb_mlp_prepare(_p(signals), n, self.nin, _p(x), ldx, _p(snorm), _p(params), self.nout,
+        rc = _lib.lib().pcgb_mlp_prepare(_p(signals), n, self.nin, int(self.log_in), _p(x), ldx, _p(snorm),
+                                         _p(params), self.nout,
                                          _p(kinds) if t is not None else None, _p(mean) if t is not None else None,
                                          _p(std) if t is not None else None, _p(t), 8, _stream())
         _lib.check("pcgb_mlp_prepare", rc)
@@ -260,7 +266,8 @@ class WarmStartMLP:
         kinds = (ctypes.c_int * self.nout)(*self.kinds)
         fl = lambda v: (ctypes.c_float * self.nout)(*[float(x) for x in v])  # noqa: E731
         with torch.cuda.device(signals.device):
-            rc = _lib.lib().pcgb_mlp_forward(_p(signals), n, self.nin, wb, wm, self.nout, kinds, fl(self.mean),
+            rc = _lib.lib().pcgb_mlp_forward(_p(signals), n, self.nin, int(self.log_in), wb, wm, self.nout, kinds,
+                                             fl(self.mean),
                                              fl(self.std), fl(self.lb), fl(self.ub), _p(out), _stream())
         _lib.check("pcgb_mlp_forward", rc)
         return out

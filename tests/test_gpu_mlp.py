@@ -72,16 +72,18 @@ def test_gradients_match_oracle():
         assert rel < 1e-2 and cos > 0.9999, (li, rel, cos)
 
 
-def test_fused_inference_matches_oracle():
+@pytest.mark.parametrize("log_in", [False, True])
+def test_fused_inference_matches_oracle(log_in):
     B = 3000
     w, data, true = _ivim16_batch(B, seed=1)
-    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, DEV, seed=4)
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, DEV, seed=4, log_in=log_in)
     sig = torch.from_numpy(data).to(DEV)
     net.fit_normalisation(sig, torch.from_numpy(true).to(DEV))
     out = net.infer(sig)
     torch.cuda.synchronize()
     smax = data.max(axis=0)
-    x = mo.bf16(data.T / smax[:, None])
+    x = data.T / smax[:, None]
+    x = mo.bf16(np.log(np.maximum(x, 1e-6)) if log_in else x)
     dims = [(16, HID), (HID, HID), (HID, HID), (HID, 4)]
     _, _, y = mo.forward(x, [L.master.cpu().numpy() for L in net.layers], dims)
     t = y * net.std + net.mean
