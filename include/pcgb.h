@@ -225,6 +225,39 @@ int pcgb_multi_run(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, 
                    double tol, double mu, double eta, double acc, double dec, int chunk, int grid,
                    uint32_t* work_counter, void* stream);
 
+/*
+ * pcgb_multi_run for callers that cannot allocate device memory. No reference
+ * counterpart: the reference always allocates its buffers through CuPy.
+ *
+ * Who needs it: code that runs while a CUDA graph is being captured (a
+ * cudaMalloc there breaks the capture), hosts whose device memory belongs to
+ * another framework's pool allocator, and embedded callers that may not grow
+ * device memory after start-up. pcgb_multi_run needs one word of device
+ * scratch (the work counter); this variant uses a statically allocated
+ * 256-byte array owned by the library instead, so it allocates nothing and
+ * calls no allocating routine. The caller still passes every input and output
+ * (the jobs' buffers).
+ *
+ * Limits and rules:
+ *  - at most 2^31 chunks of `chunk` voxels per call (summed over the jobs);
+ *    larger requests fail with PCGB_ERANGE and a message;
+ *  - every GPU that loads the library holds the 256-byte array until the
+ *    process exits;
+ *  - all calls share the array: the counter is cleared at the start of each
+ *    call (cudaMemsetAsync on the call's stream), and calls that overlap on
+ *    the GPU (concurrent streams, or several host threads) race on it, so
+ *    serialise them;
+ *  - the first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress, with that device current); make that first call
+ *    before any stream capture.
+ */
+int pcgb_multi_run_noalloc(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, const int* order, int iters,
+                           double tol, double mu, double eta, double acc, double dec, int chunk, int grid,
+                           void* stream);
+
+/* Last error of pcgb_multi_run_noalloc on this host thread. */
+const char* pcgb_noalloc_last_error(void);
+
 /* ---- fit pipeline (no reference counterpart) -------------------------------
  * fp32 structure-of-arrays buffers; values/lb/ub are host arrays of nparam.
  */

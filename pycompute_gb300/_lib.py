@@ -55,6 +55,9 @@ SIGNATURES = {
     "pcgb_multi_grid": (c_int, [c_void_p]),
     "pcgb_multi_run": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_double, c_double, c_double, c_double,
                                c_double, c_int, c_int, c_void_p, c_void_p]),
+    "pcgb_multi_run_noalloc": (c_int, [c_void_p, c_void_p, c_int, c_void_p, c_int, c_double, c_double, c_double,
+                                       c_double, c_double, c_int, c_int, c_void_p]),
+    "pcgb_noalloc_last_error": (c_char_p, []),
     "pcgb_model_eval": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_int, c_void_p]),
     "pcgb_pipeline_last_error": (c_char_p, []),
     "pcgb_init_constant": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p]),
@@ -115,6 +118,8 @@ def check(fn_name: str, rc: int):
         L = lib()
         if fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")):
             err = L.pcgb_mlp_last_error
+        elif fn_name.startswith("pcgb_multi_run_noalloc"):
+            err = L.pcgb_noalloc_last_error
         elif fn_name.startswith(("pcgb_init_constant", "pcgb_fallback", "pcgb_bpolyfit", "pcgb_ivim")):
             err = L.pcgb_pipeline_last_error
         else:
