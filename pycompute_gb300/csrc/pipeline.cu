@@ -334,7 +334,7 @@ int pcgb_bpolyfit(const float* x, int64_t x_stride, const double* x_shared, cons
   a.deg = deg;
   a.log_y = log_y;
   a.out = out;
-  bpolyfit_kernel<<<blocks(n), 128, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  bpolyfit_kernel<<<unsigned((n + 127) / 128), 128, 0, static_cast<cudaStream_t>(stream)>>>(a);
   return cuda_rc();
 }
 

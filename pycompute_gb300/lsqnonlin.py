@@ -145,30 +145,31 @@ def _model_from(model_expr, f_gradf, legacy) -> tuple[str, str, int, int, str, O
     raise RuntimeError("One and only one of model_expr or f_gradf must be non None")
 
 
-_host_copies: dict = {}
+def _shared_rows(t, rows: int, n: int, name: str, detect: bool):
+    """Classify a protocol/bounds argument: (device tensor or None, stride, host values).
 
-
-def _host_values(t: torch.Tensor) -> list:
-    """Host copy of a small shared protocol/bounds column, cached per tensor
-    version so repeated setup() calls with the same tensor need no sync."""
-    key = (t.data_ptr(), t.dtype, tuple(t.shape), t._version)
-    v = _host_copies.get(key)
-    if v is None:
-        v = t.reshape(-1).double().cpu().tolist()
-        if len(_host_copies) > 64:
-            _host_copies.clear()
-        _host_copies[key] = v
-    return v
-
-
-def _shared_rows(t: torch.Tensor, rows: int, n: int, name: str, detect: bool):
-    """Classify a (rows, N) / (rows, 1) / (rows,) tensor: (tensor, stride, host values)."""
+    A host sequence (list, tuple, numpy array, CPU tensor) of ``rows`` values
+    is a shared protocol and costs no device access; a (rows, 1) / (rows,)
+    CUDA tensor is shared too (read back once); a (rows, N) CUDA tensor is per
+    voxel unless ``detect`` finds all its columns equal.
+    """
+    if not isinstance(t, torch.Tensor) and not hasattr(t, "__dlpack__"):
+        vals = [float(x) for x in (t.reshape(-1) if hasattr(t, "reshape") else t)]
+        if len(vals) != rows:
+            raise RuntimeError(f"{name} must have {rows} values, got {len(vals)}")
+        return None, 0, vals
+    t = _as_tensor(t, name)
+    if not t.is_cuda:
+        vals = t.reshape(-1).double().tolist()
+        if len(vals) != rows:
+            raise RuntimeError(f"{name} must have {rows} values, got {len(vals)}")
+        return None, 0, vals
     if t.dim() == 1:
         t = t.reshape(rows, 1)
     if t.dim() != 2 or t.shape[0] != rows:
         raise RuntimeError(f"{name} must have {rows} rows, got shape {tuple(t.shape)}")
     if t.shape[1] == 1 and n != 1:
-        return t, 0, _host_values(t[:, 0])
+        return t, 0, t[:, 0].double().cpu().tolist()
     if t.shape[1] != n:
         raise RuntimeError(f"{name} must have 1 or {n} columns, got {t.shape[1]}")
     if detect and n > 0 and bool((t == t[:, :1]).all()):
@@ -262,15 +263,14 @@ class SecondOrderLevenbergMarquardt:
         """Bind caller-owned arrays and allocate the fitter state (lsqnonlin.py:1036-1056)."""
         pars_t = _as_tensor(pars_t, "pars_t")
         data_t = _as_tensor(data_t, "data_t")
-        consts_t = _as_tensor(consts_t, "consts_t")
-        lower_bound_t = _as_tensor(lower_bound_t, "lower_bound_t")
-        upper_bound_t = _as_tensor(upper_bound_t, "upper_bound_t")
         P, M, C = self.nparam, self.ndata, self.nconst
         if data_t.dim() != 2 or data_t.shape[0] != M:
             raise RuntimeError(f"data_t must be ({M}, N), got {tuple(data_t.shape)}")
         N = int(data_t.shape[1])
         for name, t in (("pars_t", pars_t), ("data_t", data_t), ("consts_t", consts_t),
                         ("lower_bound_t", lower_bound_t), ("upper_bound_t", upper_bound_t)):
+            if not isinstance(t, torch.Tensor) or (name not in ("pars_t", "data_t") and not t.is_cuda):
+                continue  # host protocol / bounds values
             if not t.is_cuda:
                 raise RuntimeError(f"{name} must be a CUDA tensor")
             if t.dtype != self.dtype:
@@ -287,10 +287,16 @@ class SecondOrderLevenbergMarquardt:
         self.lower_bound_t, bs_l, lbv = _shared_rows(lower_bound_t, P, N, "lower_bound_t", self.detect_shared)
         self.upper_bound_t, bs_u, ubv = _shared_rows(upper_bound_t, P, N, "upper_bound_t", self.detect_shared)
         if bs_l != bs_u:
-            if bs_l == 0:
-                self.lower_bound_t, bs_l, lbv = _shared_rows(lower_bound_t.expand(P, N).contiguous(), P, N, "lb", False)
-            if bs_u == 0:
-                self.upper_bound_t, bs_u, ubv = _shared_rows(upper_bound_t.expand(P, N).contiguous(), P, N, "ub", False)
+            dev = pars_t.device
+
+            def per_voxel(vals, t):
+                if vals is not None:
+                    return torch.tensor(vals, dtype=self.dtype, device=dev)[:, None].expand(P, N).contiguous()
+                return t
+            lt = per_voxel(lbv, self.lower_bound_t)
+            ut = per_voxel(ubv, self.upper_bound_t)
+            self.lower_bound_t, bs_l, lbv = lt, N, None
+            self.upper_bound_t, bs_u, ubv = ut, N, None
         self._bstride = bs_l
         self._lb_host, self._ub_host = lbv, ubv
         dev = pars_t.device
@@ -509,10 +515,15 @@ class RandomSearch:
         data_t = _as_tensor(data_t, "data_t")
         N = int(data_t.shape[1])
         self.Nprobs = N
-        lbt = _as_tensor(lower_bound_t, "lower_bound_t")
-        self.best_pars_t = lbt.reshape(self.nparam, -1).expand(self.nparam, N).contiguous().clone()
+        lm = self._lm
+        lm.setup(torch.empty((self.nparam, N), dtype=self.dtype, device=data_t.device), consts_t, data_t,
+                 lower_bound_t, upper_bound_t)
+        if lm._bstride == 0:
+            lbv = torch.tensor(lm._lb_host, dtype=self.dtype, device=data_t.device)
+            self.best_pars_t = lbv[:, None].expand(self.nparam, N).contiguous()
+        else:
+            self.best_pars_t = lm.lower_bound_t.clone()
         self.best_f_t = torch.full((1, N), torch.finfo(self.dtype).max / 5, dtype=self.dtype, device=data_t.device)
-        self._lm.setup(self.best_pars_t.clone(), consts_t, data_t, lower_bound_t, upper_bound_t)
 
     def run(self, iters: int, lm_iters: int | None = None, tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0,
             seed: int | None = None):

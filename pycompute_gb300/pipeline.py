@@ -96,11 +96,9 @@ class WarmStartFitter:
         return self._solm
 
     def _consts(self, dev):
-        if dev not in self._dev_consts:
-            w = self.w
-            self._dev_consts[dev] = tuple(torch.tensor(x, dtype=torch.float32, device=dev)
-                                          for x in (w.protocol, w.lb, w.ub))
-        return self._dev_consts[dev]
+        # shared protocol and bounds as host values: setup() needs no device read-back
+        w = self.w
+        return list(w.protocol), list(w.lb), list(w.ub)
 
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
             lam0: float = 1e-3, timings: dict | None = None):
