@@ -203,7 +203,7 @@ def fp64_reference(w, data, iters=1000):
     return p
 
 
-def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=64, seed=77, lam0=1e-3):
+def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=64, seed=77, lam0=3e-3):
     """C5: IVIM-16, MLP warm start + LM + fallback vs plain LM, fits/s at 1e-4 vs FP64."""
     import torch
     from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline, synth
@@ -380,7 +380,7 @@ def main():
     ap.add_argument("--only-mixed", action="store_true", help="run only the mixed-model batch comparison")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--warm-epochs", type=int, default=64)
-    ap.add_argument("--warm-lam0", type=float, default=1e-3)
+    ap.add_argument("--warm-lam0", type=float, default=3e-3)
     ap.add_argument("--warm-train", type=int, default=1 << 21)
     args = ap.parse_args()
     if args.impl == "reference":
@@ -397,6 +397,8 @@ def main():
     import torch.distributed as dist
 
     from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, parity, synth
+
+    from pycompute_gb300.shard import max_over_ranks
 
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
@@ -453,10 +455,7 @@ def main():
         dist.barrier()
     step_ms = t_start.elapsed_time(t_end) / args.steps
     kern_ms = statistics.mean(k_start[s].elapsed_time(k_end[s]) for s in range(args.steps))
-    if ws > 1:
-        t = torch.tensor([step_ms, kern_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        step_ms, kern_ms = float(t[0]), float(t[1])
+    step_ms, kern_ms = max_over_ranks([step_ms, kern_ms], device=dev)
     fitted = pars_d.cpu().numpy()
     st = solm.step_type_t.cpu().numpy()[0]
     its = solm.iters_t.cpu().numpy()[0].astype(np.int64)
@@ -490,11 +489,7 @@ def main():
         e2e_step()
     e_end.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e_start.elapsed_time(e_end) / args.steps
-    if ws > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t[0])
+    e2e_ms = max_over_ranks([e_start.elapsed_time(e_end) / args.steps], device=dev)[0]
     assert np.array_equal(out_pars_h.numpy(), fitted), "e2e result differs from the device-resident run"
     h2d = data.nbytes + init.nbytes
     d2h = init.nbytes + N

@@ -248,3 +248,19 @@ def test_input_validation_raises():
         solm.setup(_t(init[:3]), _t(prot), _t(data), _t(lb), _t(ub))
     with pytest.raises(RuntimeError):
         solm.run(10)
+
+
+def test_user_supplied_model_code_f_gradf():
+    """F_GradF (lsqnonlin.py:32-39): a fit from user-supplied model code equals the Expr fit."""
+    from pycompute_gb300 import F_GradF, codegen
+    w = synth.ivim()
+    true, data, init, lb, ub, prot = w.generate(3000, seed=12)
+    gm = codegen.generate(w.expr, w.pars, w.consts, struct_name="UserIvim")
+    a, _ = fit_gpu(w, data, init, lb, ub, prot, 40)
+    solm = SecondOrderLevenbergMarquardt(None, F_GradF(gm.source, 4, 1, "UserIvim"), w.M, torch.float32)
+    p = _t(init)
+    solm.setup(p, _t(prot), _t(data), _t(lb), _t(ub))
+    solm.run(40)
+    torch.cuda.synchronize()
+    assert solm.funcid.endswith("_UserIvim")
+    np.testing.assert_array_equal(p.cpu().numpy(), a["pars"])
