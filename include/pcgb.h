@@ -125,6 +125,62 @@ int pcgb_lm_run_subset(pcgb_fitter* fitter, const void* consts, int64_t consts_s
                        int block, const int32_t* vox_idx, int64_t n_items, void* stream);
 
 /*
+ * pcgb_lm_run with the refill schedule: a persistent grid in which every lane
+ * fits one voxel at a time and, when its voxel converges or runs out of
+ * iterations, takes the next one (warp ballot + prefix-sum rank; warps claim
+ * 256-voxel chunks from work_counter). Per-voxel results equal pcgb_lm_run's;
+ * it is faster when voxels converge after very different numbers of
+ * iterations. vox_idx / n_items restrict the fit to a list as in
+ * pcgb_lm_run_subset (vox_idx may be NULL). n_items_dev (may be NULL; needs
+ * vox_idx): a device word holding the list length, of which the first
+ * min(*n_items_dev, n_items) entries are fitted, so a compaction's count needs
+ * no host round trip. work_counter: one uint32 of device scratch, zeroed by
+ * this call; grid <= 0 selects the persistent grid.
+ * No reference counterpart (the reference launches one thread per voxel per
+ * iteration).
+ */
+int pcgb_lm_run_refill(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                       void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                       const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                       int block, const int32_t* vox_idx, int64_t n_items, const uint32_t* n_items_dev,
+                       uint32_t* work_counter, int grid, void* stream);
+
+/*
+ * Fallback check of a warm-started fit, fused per model (no reference
+ * counterpart; it implements the rule "refit from the plain fitter's start
+ * where the warm fit fails to lower the cost below that start's or lands on a
+ * bound"). In one pass over the samples of every voxel: cost[v] = cost at
+ * params; the voxel is flagged if that cost is not finite, not below the cost
+ * at the constant start (init_values, P host values, NaN = the voxel's largest
+ * sample), or a parameter is not strictly inside [lb, ub]. Flagged voxels are
+ * appended to fb_idx (order unspecified) with fb_count[0] their number; their
+ * warm fit goes to pars_backup (P, nprobs; column i = i-th flagged voxel) and
+ * cost_backup, their params are set to the constant start, lam to lam0,
+ * step_type to 1 and f to 0, ready for pcgb_lm_run_refill on
+ * (fb_idx, n_items_dev = fb_count). fb_count: two uint32 of device memory,
+ * zeroed by this call. nprobs < 2^31.
+ */
+int pcgb_warm_check(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                    const void* lower_bound, const void* upper_bound, int64_t bounds_stride,
+                    const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                    const double* init_values, double lam0, void* params, void* lam, int8_t* step_type, void* f,
+                    void* cost, void* pars_backup, void* cost_backup, int32_t* fb_idx, uint32_t* fb_count,
+                    int64_t nprobs, void* stream);
+
+/*
+ * After the refit of the flagged voxels: for each of the fb_count[0] voxels of
+ * fb_idx, the cost at its refitted params is compared with cost_backup; the
+ * lower fit is kept in params and cost, fb_count[1] counts the kept refits,
+ * which[v] (may be NULL) = 1 where the refit was kept.
+ */
+int pcgb_warm_select(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                     const double* protocol_host, int protocol_len, void* params, void* cost, const void* pars_backup,
+                     const void* cost_backup, const int32_t* fb_idx, uint32_t* fb_count, int8_t* which,
+                     int64_t nprobs, void* stream);
+
+/*
  * Accumulating objective f[v] += sum_i (m(p_v; c_i) - d_i)^2, voxels whose
  * step_type is 0 skipped (step_type may be NULL). Replaces F.run
  * (lsqnonlin.py:137-145; kernel lsqnonlin.py:160-172).
@@ -265,6 +321,12 @@ const char* pcgb_noalloc_last_error(void);
 /* Last error of the pipeline entry points on this host thread. */
 const char* pcgb_pipeline_last_error(void);
 
+/* y[i] = 1/x[i] by the FP64 reciprocal of the FP64 GMW81 solve (float seed and
+ * two Newton-Raphson steps; zero, Inf, NaN and exponents outside the float
+ * range take the correctly rounded reciprocal). Within 1 ulp of 1/x; exposed
+ * so callers and tests can check that bound on their own inputs. */
+int pcgb_rcp64(const double* x, double* y, int64_t n, void* stream);
+
 /* Constant initialisation: pars[k][v] = values[k]; a NaN entry means "the
  * voxel's largest sample" (the reference notebooks' S0 start). */
 int pcgb_init_constant(const float* data, int64_t n, int m, int nparam, const double* values, float* pars,
@@ -365,6 +427,18 @@ int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, int log_in, void*
 int pcgb_mlp_forward(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
                      const float* const* w_master, int nout, const int* kinds, const float* mean, const float* stdv, const float* lb,
                      const float* ub, float* out, void* stream);
+
+/* pcgb_mlp_forward on the tcgen05 tensor cores: one CTA per SM with four
+ * 128-voxel tiles in flight, layer accumulators in tensor memory, operands in
+ * shared memory. Same arguments and results (up to fp32 summation order);
+ * status (device int, may be NULL) is set to 1 if the kernel gave up on a
+ * bounded wait for its tensor-core work (its outputs are then incomplete). */
+int pcgb_mlp_forward_tc(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
+                        const float* const* w_master, int nout, const int* kinds, const float* mean, const float* stdv,
+                        const float* lb, const float* ub, float* out, int* status, void* stream);
+
+/* Last error of pcgb_mlp_forward_tc on this host thread. */
+const char* pcgb_mlp_tc_last_error(void);
 
 #ifdef __cplusplus
 }

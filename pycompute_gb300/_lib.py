@@ -38,6 +38,15 @@ SIGNATURES = {
                                    c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_int, c_void_p, c_int, c_void_p,
                                    c_void_p, c_int, c_void_p, c_i64, c_void_p]),
+    "pcgb_lm_run_refill": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_double,
+                                   c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_int, c_void_p, c_int, c_void_p,
+                                   c_void_p, c_int, c_void_p, c_i64, c_void_p, c_void_p, c_int, c_void_p]),
+    "pcgb_warm_check": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_int,
+                                c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
+                                c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+    "pcgb_warm_select": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
+                                 c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
     "pcgb_f_run_subset": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64,
                                   c_void_p, c_int, c_void_p, c_i64, c_void_p]),
     "pcgb_f_run": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p,
@@ -60,6 +69,7 @@ SIGNATURES = {
     "pcgb_noalloc_last_error": (c_char_p, []),
     "pcgb_model_eval": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_int, c_void_p]),
     "pcgb_pipeline_last_error": (c_char_p, []),
+    "pcgb_rcp64": (c_int, [c_void_p, c_void_p, c_i64, c_void_p]),
     "pcgb_init_constant": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "pcgb_bpolyfit": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_i64, c_int, c_int, c_int, c_int, c_void_p,
                               c_void_p]),
@@ -82,6 +92,9 @@ SIGNATURES = {
                                  c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
     "pcgb_mlp_forward": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pcgb_mlp_forward_tc": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+                                    c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pcgb_mlp_tc_last_error": (c_char_p, []),
 }
 
 
@@ -116,11 +129,13 @@ def lib(build_if_missing: bool = True):
 def check(fn_name: str, rc: int):
     if rc != 0:
         L = lib()
-        if fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")):
+        if fn_name.startswith("pcgb_mlp_forward_tc"):
+            err = L.pcgb_mlp_tc_last_error
+        elif fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")):
             err = L.pcgb_mlp_last_error
         elif fn_name.startswith("pcgb_multi_run_noalloc"):
             err = L.pcgb_noalloc_last_error
-        elif fn_name.startswith(("pcgb_init_constant", "pcgb_fallback", "pcgb_bpolyfit", "pcgb_ivim")):
+        elif fn_name.startswith(("pcgb_init_constant", "pcgb_rcp64", "pcgb_fallback", "pcgb_bpolyfit", "pcgb_ivim")):
             err = L.pcgb_pipeline_last_error
         else:
             err = L.pcgb_last_error

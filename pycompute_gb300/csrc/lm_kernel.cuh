@@ -61,6 +61,7 @@ template <> struct Num<float> {
   static PCGB_HD float prot(const PcgbLmParams& a, int i) { return a.protocol_f[i]; }
   static PCGB_HD float slb(const PcgbLmParams& a, int k) { return a.shared_lb_f[k]; }
   static PCGB_HD float sub(const PcgbLmParams& a, int k) { return a.shared_ub_f[k]; }
+  static PCGB_HD float inf() { return __int_as_float(0x7f800000); }
 };
 template <> struct Num<double> {
   static PCGB_HD double gmw_eps() { return 4e-16; }   // solver.py:109
@@ -68,6 +69,7 @@ template <> struct Num<double> {
   static PCGB_HD double prot(const PcgbLmParams& a, int i) { return a.protocol_d[i]; }
   static PCGB_HD double slb(const PcgbLmParams& a, int k) { return a.shared_lb_d[k]; }
   static PCGB_HD double sub(const PcgbLmParams& a, int k) { return a.shared_ub_d[k]; }
+  static PCGB_HD double inf() { return __longlong_as_double(0x7ff0000000000000LL); }
 };
 
 PCGB_HD constexpr int pk(int i, int j) { return i * (i + 1) / 2 + j; }  // packed lower index, j <= i
@@ -217,6 +219,26 @@ PCGB_HD double widen(float x) {
   return static_cast<double>(x);
 }
 
+// 1/x in FP64 by Newton-Raphson iteration (Markstein, IBM J. Res. Dev. 34,
+// 1990): a float seed from the float reciprocal of x's truncated high word
+// (relative error < 2^-19), then two steps y <- y + y (1 - x y), each squaring
+// the error (< 2^-76 < 2^-53). 4 DFMA in place of the ~11 FP64-pipe
+// instructions of the correctly rounded reciprocal, within 1 ulp of it.
+// Exponents whose float seed or its reciprocal would leave the normal float
+// range (and zero, Inf, NaN) take the hardware reciprocal.
+PCGB_HD double rcp64(double x) {
+  const unsigned hi = static_cast<unsigned>(__double2hiint(x));
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e - 897u >= 252u) return __drcp_rn(x);
+  const unsigned fb = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3);
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(__uint_as_float(fb)));
+  double y = widen(r);
+  y = fma(y, fma(-x, y, 1.0), y);
+  y = fma(y, fma(-x, y, 1.0), y);
+  return y;
+}
+
 // A: packed fp32 matrix (row i, column j <= i), b: fp32 right-hand side.
 template <int P>
 PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const float (&b)[P], double (&x)[P]) {
@@ -251,7 +273,7 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
   unsigned long long bb = 0x3CBCD2B297D889BCULL;  // 4e-16, solver.py:109
   if (abs_bits(gam) > bb) bb = abs_bits(gam);
   if (abs_bits(nu) > bb) bb = abs_bits(nu);
-  const double inv_beta2 = __drcp_rn(from_bits(bb));
+  const double inv_beta2 = rcp64(from_bits(bb));
   const double gn = gam + nu;
   const double delta = gn > 1.0 ? 4e-16 * gn : 4e-16;
 
@@ -271,14 +293,16 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
     unsigned long long tb = 0;
 #pragma unroll
     for (int i = j + 1; i < P; ++i) max_abs_bits(tb, c[i][j]);
-    const double th = from_bits(tb);
-    const double th2 = (th * th) * inv_beta2;
     // d = max(|c_jj|, delta, theta^2 / beta^2); a NaN c_jj falls through like the reference
     const unsigned long long cj = abs_bits(c[j][j]);
     double d = cj > 0x7ff0000000000000ULL ? c[j][j] : from_bits(cj);
     if (abs_bits(d) < abs_bits(delta)) d = delta;
-    if (abs_bits(d) < abs_bits(th2)) d = th2;
-    inv_d[j] = __drcp_rn(d);
+    if (j + 1 < P) {  // the last column has no sub-diagonal entries: theta = 0
+      const double th = from_bits(tb);
+      const double th2 = (th * th) * inv_beta2;
+      if (abs_bits(d) < abs_bits(th2)) d = th2;
+    }
+    inv_d[j] = rcp64(d);
 #pragma unroll
     for (int i = j + 1; i < P; ++i) c[i][i] = fma(-c[i][j], c[i][j] * inv_d[j], c[i][i]);
   }
@@ -302,6 +326,7 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
 }
 
 template <typename T> PCGB_HD T load(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
+template <typename T> PCGB_HD T load_(const void* p, long long i) { return static_cast<const T*>(p)[i]; }
 
 template <typename A, typename B> struct SameType { static constexpr bool value = false; };
 template <typename A> struct SameType<A, A> { static constexpr bool value = true; };
@@ -442,8 +467,8 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
       const bool pzero = pb == 0;                         // +0: rho = +Inf
       const bool pos = pb > 0;                            // > +0 (NaN has the sign bit or is > +Inf bits)
       const bool up = f > ftp;                            // actual > 0
-      accept = up && ((pos && pb < 0x7ff0000000000000LL && actual > double(mu) * pred) || pzero);
-      very_good = pzero || actual > double(eta) * pred;
+      accept = up && ((pos && pb < 0x7ff0000000000000LL && actual > widen(mu) * pred) || pzero);
+      very_good = pzero || actual > widen(eta) * pred;
       pred_neg = pred < 0.0;
     } else {
       const TS actual = TS(0.5) * (TS(f) - TS(ftp));
@@ -565,6 +590,158 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
   if (a.iters_done) a.iters_done[v] += done;
 }
 
+// ---- refill schedule -----------------------------------------------------------
+//
+// One voxel per lane at a time, one LM iteration per pass: after every pass
+// the warp ballots the lanes whose voxel has finished (converged or out of
+// iterations), stores them, and hands those lanes the next voxels of the
+// warp's chunk by their prefix-sum rank in the ballot. A warp whose chunk is
+// drained claims the next chunk of the launch's work counter (one atomic per
+// chunk). Lanes therefore never idle behind a slower voxel of their warp
+// while work remains; each voxel's arithmetic is the grid schedule's.
+
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+struct VoxelFit {
+  static constexpr int P = Model::P, C = Model::C;
+  TA p[P], lo[P], hi[P], stp[P], d[M];
+  TA cv[SHARED_C ? 1 : (C > 0 ? C * M : 1)];
+  TA lam, f, first;
+  int st, done, it;
+
+  // false when the voxel was converged before the call (its outputs are then
+  // already written, as in lm_fit_voxel)
+  PCGB_HD bool load(const PcgbLmParams& a, long long v) {
+    const long long N = a.N;
+    if (a.step_type[v] == 0) {
+      if (a.iters > 0) {
+        const TA f0 = load_<TA>(a.f, v);
+        static_cast<TA*>(a.first_f)[v] = f0;
+        static_cast<TA*>(a.last_f)[v] = f0;
+      }
+      return false;
+    }
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      p[k] = load_<TA>(a.pars, k * N + v);
+      lo[k] = SHARED_B ? Num<TA>::slb(a, k) : load_<TA>(a.lb, k * a.bstride + v);
+      hi[k] = SHARED_B ? Num<TA>::sub(a, k) : load_<TA>(a.ub, k * a.bstride + v);
+      stp[k] = a.step ? load_<TA>(a.step, k * N + v) : TA(0);
+    }
+#pragma unroll
+    for (int i = 0; i < M; ++i) d[i] = load_<TA>(a.data, i * N + v);
+    if (!SHARED_C) {
+#pragma unroll
+      for (int i = 0; i < C * M; ++i) cv[i] = load_<TA>(a.consts, i * a.cstride + v);
+    }
+    lam = load_<TA>(a.lam, v);
+    st = a.step_type[v];
+    f = load_<TA>(a.f, v);
+    first = f;
+    done = 0;
+    it = 0;
+    return true;
+  }
+
+  PCGB_HD bool finished(const PcgbLmParams& a) const { return st == 0 || it >= a.iters; }
+
+  PCGB_HD void step(const PcgbLmParams& a) {
+    const TA tol = TA(a.tol), mu = TA(a.mu), eta = TA(a.eta), acc = TA(a.acc), dec = TA(a.dec);
+    TA first_it = first;
+    if constexpr (SHARED_C) {
+      lm_iterate<Model, M, TA, TS>(SharedConsts<TA, M>{a}, d, p, lo, hi, stp, lam, st, f, first_it, done, 1, tol, mu,
+                                   eta, acc, dec);
+    } else {
+      lm_iterate<Model, M, TA, TS>(RegConsts<TA, M, (C > 0 ? C * M : 1)>{cv}, d, p, lo, hi, stp, lam, st, f,
+                                   first_it, done, 1, tol, mu, eta, acc, dec);
+    }
+    if (it == 0) first = first_it;
+    ++it;
+  }
+
+  PCGB_HD void store(const PcgbLmParams& a, long long v) const {
+    const long long N = a.N;
+    TA* pars = static_cast<TA*>(a.pars);
+#pragma unroll
+    for (int k = 0; k < P; ++k) pars[k * N + v] = p[k];
+    if (a.step) {
+#pragma unroll
+      for (int k = 0; k < P; ++k) static_cast<TA*>(a.step)[k * N + v] = stp[k];
+    }
+    static_cast<TA*>(a.lam)[v] = lam;
+    a.step_type[v] = static_cast<signed char>(st);
+    static_cast<TA*>(a.f)[v] = f;
+    if (a.iters > 0) {
+      static_cast<TA*>(a.first_f)[v] = first;
+      static_cast<TA*>(a.last_f)[v] = f;
+    }
+    if (a.iters_done) a.iters_done[v] += done;
+  }
+};
+
+// Refill schedule over work items [begin, end) and, when `claim` is set,
+// further chunks of `chunk` items claimed from a.work. The cursor `next` and
+// the range are warp-uniform; idle lanes take items by their rank among the
+// idle lanes.
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+__device__ void lm_refill(const PcgbLmParams& a, long long begin, long long end, bool claim, long long chunk,
+                          long long n_items) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  VoxelFit<Model, M, TA, TS, SHARED_C, SHARED_B> s;
+  bool active = false;
+  long long v = 0;
+  long long next = begin;
+  for (;;) {
+    for (;;) {  // hand work to idle lanes while there is any
+      const unsigned idle = __ballot_sync(0xffffffffu, !active);
+      if (idle == 0u) break;
+      if (next >= end) {
+        if (!claim) break;
+        unsigned int c = 0;
+        if (lane == 0) c = atomicAdd(a.work, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        next = (long long)c * chunk;
+        if (next >= n_items) {
+          claim = false;
+          break;
+        }
+        end = next + chunk < n_items ? next + chunk : n_items;
+      }
+      const long long avail = end - next;
+      const int nidle = __popc(idle);
+      const int take = (long long)nidle < avail ? nidle : int(avail);
+      const int my = __popc(idle & lt);
+      if (!active && my < take) {
+        const long long item = next + my;
+        v = a.vox_idx ? (long long)a.vox_idx[item] : item;
+        active = s.load(a, v);  // a voxel converged before this call is done at once
+      }
+      next += take;
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (active) {
+      if (!s.finished(a)) s.step(a);
+      if (s.finished(a)) {
+        s.store(a, v);
+        active = false;
+      }
+    }
+  }
+}
+
+// Single-model refill kernel body: every warp starts on an empty range and
+// claims chunks of 8 items per lane from a.work. The item count may come from
+// device memory (a compaction's counter), so the launch needs no host sync.
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+__device__ void lm_refill_grid(const PcgbLmParams& a) {
+  long long n = a.n_items;
+  if (a.n_items_dev) {
+    const long long d = (long long)*a.n_items_dev;
+    n = d < n ? d : n;
+  }
+  lm_refill<Model, M, TA, TS, SHARED_C, SHARED_B>(a, 0, 0, true, 256, n);
+}
+
 // Grid-stride schedule: thread t fits work items t, t + T, t + 2T, ...; an
 // item is a voxel index, or an entry of the compacted list vox_idx.
 template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
@@ -640,6 +817,132 @@ __device__ void eval_grid(const PcgbLmParams& a) {
         c[k] = SHARED_C ? Num<TA>::prot(a, k * M + i) : load<TA>(a.consts, (k * M + i) * a.cstride + v);
       static_cast<TA*>(a.model_out)[i * a.N + v] = Model::template value<TA>(p, c);
     }
+  }
+}
+
+// ---- fallback of a warm-started fit -------------------------------------------
+//
+// A warm-started fit is refitted from the plain fitter's constant start where
+// its cost is not finite, not below the cost at that start, or where it ends
+// on a bound. warm_check_grid decides this for every voxel in one pass over
+// its samples (both costs from registers), compacts the flagged voxels with
+// one atomic per warp, saves their warm fits and resets their fitter state to
+// the constant start. The refit then runs on the compacted list with the
+// count read from device memory, and warm_select_grid keeps, per flagged
+// voxel, whichever of the two fits has the lower cost. No step needs the
+// flagged count on the host.
+
+// sum_i (m(p; c_i) - d_i)^2, in the order of cost_grid
+template <class Model, int M, typename TA, class CF>
+PCGB_HD TA sum_sq_residual(const CF& cf, const TA (&p)[Model::P], const TA (&d)[M]) {
+  constexpr int C = Model::C;
+  TA s = TA(0);
+#pragma unroll
+  for (int i = 0; i < M; ++i) {
+    TA c[C > 0 ? C : 1];
+#pragma unroll
+    for (int k = 0; k < C; ++k) c[k] = cf(k, i);
+    const TA r = Model::template value<TA>(p, c) - d[i];
+    s += r * r;
+  }
+  return s;
+}
+
+template <class Model, int M, typename TA, bool SHARED_C>
+PCGB_HD TA voxel_cost(const PcgbLmParams& a, long long v, const TA (&p)[Model::P], const TA (&d)[M]) {
+  constexpr int C = Model::C;
+  if constexpr (SHARED_C) {
+    return sum_sq_residual<Model, M, TA>(SharedConsts<TA, M>{a}, p, d);
+  } else {
+    TA cv[C > 0 ? C * M : 1];
+#pragma unroll
+    for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
+    return sum_sq_residual<Model, M, TA>(RegConsts<TA, M, (C > 0 ? C * M : 1)>{cv}, p, d);
+  }
+}
+
+// one thread per voxel, grid covering N (every lane reaches the ballot)
+template <class Model, int M, typename TA, bool SHARED_C>
+__device__ void warm_check_grid(const PcgbLmParams& a) {
+  constexpr int P = Model::P;
+  const long long N = a.N;
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  bool flag = false;
+  TA p[P], p0[P], c = TA(0);
+  if (v < N) {
+    TA d[M];
+    TA mx = -Num<TA>::inf();
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+      d[i] = load<TA>(a.data, i * N + v);
+      mx = fmax(mx, d[i]);
+    }
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      p[k] = load<TA>(a.pars, k * N + v);
+      p0[k] = isnan(a.init_val[k]) ? mx : TA(a.init_val[k]);
+    }
+    c = voxel_cost<Model, M, TA, SHARED_C>(a, v, p, d);
+    const TA c0 = voxel_cost<Model, M, TA, SHARED_C>(a, v, p0, d);
+    flag = !isfinite(c) || !(c < c0);
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+      const TA lo = a.bstride ? load<TA>(a.lb, k * a.bstride + v) : Num<TA>::slb(a, k);
+      const TA hi = a.bstride ? load<TA>(a.ub, k * a.bstride + v) : Num<TA>::sub(a, k);
+      flag = flag || !(p[k] > lo) || !(p[k] < hi);
+    }
+    static_cast<TA*>(a.cost)[v] = c;
+  }
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned ballot = __ballot_sync(0xffffffffu, flag);
+  if (!ballot) return;
+  unsigned base = 0;
+  if (lane == 0) base = atomicAdd(a.fb_count, (unsigned)__popc(ballot));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (!flag) return;
+  const long long i = (long long)base + __popc(ballot & ((1u << lane) - 1u));
+  a.fb_idx[i] = int(v);
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    static_cast<TA*>(a.pars_backup)[k * N + i] = p[k];
+    static_cast<TA*>(a.pars)[k * N + v] = p0[k];
+  }
+  static_cast<TA*>(a.cost_backup)[i] = c;
+  static_cast<TA*>(a.lam)[v] = TA(a.lam0);
+  a.step_type[v] = 1;
+  static_cast<TA*>(a.f)[v] = TA(0);
+}
+
+// grid-stride over the flagged voxels (count from a.n_items_dev)
+template <class Model, int M, typename TA, bool SHARED_C>
+__device__ void warm_select_grid(const PcgbLmParams& a) {
+  constexpr int P = Model::P;
+  const long long N = a.N;
+  long long n = a.n_items;
+  if (a.n_items_dev) {
+    const long long d = (long long)*a.n_items_dev;
+    n = d < n ? d : n;
+  }
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += T) {
+    const long long v = a.fb_idx[i];
+    TA p[P], d[M];
+#pragma unroll
+    for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * N + v);
+#pragma unroll
+    for (int s = 0; s < M; ++s) d[s] = load<TA>(a.data, s * N + v);
+    const TA c = voxel_cost<Model, M, TA, SHARED_C>(a, v, p, d);
+    const TA cb = load<TA>(a.cost_backup, i);
+    const bool refit = c < cb;
+    if (!refit) {
+#pragma unroll
+      for (int k = 0; k < P; ++k) static_cast<TA*>(a.pars)[k * N + v] = load<TA>(a.pars_backup, k * N + i);
+    }
+    static_cast<TA*>(a.cost)[v] = refit ? c : cb;
+    if (a.which) a.which[v] = refit ? 1 : 0;
+    const unsigned m = __activemask();
+    const unsigned kept = __ballot_sync(m, refit);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1) && kept) atomicAdd(a.fb_count + 1, (unsigned)__popc(kept));
   }
 }
 

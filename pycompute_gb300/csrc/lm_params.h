@@ -36,6 +36,16 @@ struct PcgbLmParams {
   int iters;
   int flags;
   double tol, mu, eta, acc, dec;
+  // fallback check of a warm-started fit (warm_check_grid / warm_select_grid)
+  const unsigned int* n_items_dev;  // when set, the work-item count is min(*n_items_dev, n_items)
+  void* cost;                       // (N) cost at the fit's final point, out
+  void* pars_backup;                // (P, N) warm fits of the flagged voxels, compacted
+  void* cost_backup;                // (N) their costs, compacted
+  int* fb_idx;                      // (N) flagged voxel indices, compacted
+  unsigned int* fb_count;           // [0] flagged voxels, [1] refits kept (zeroed by the host)
+  signed char* which;               // (N) 1 where the refit was kept, or null
+  double lam0;                      // damping of the refit
+  float init_val[PCGB_MAX_PARAMS];  // constant start of the refit; NaN = the voxel's largest sample
   // shared protocol and bounds in both precisions, so the kernel reads its own
   // type straight from the parameter bank (constant k of sample i at k*M + i)
   float shared_lb_f[PCGB_MAX_PARAMS];

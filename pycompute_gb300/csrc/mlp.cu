@@ -23,11 +23,10 @@
 #include <cstdio>
 #include <string>
 
+#include "mlp_math.cuh"
 #include "pcgb.h"
 
 namespace pcgb_mlp {
-
-using bf16 = __nv_bfloat16;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -53,30 +52,6 @@ __device__ __forceinline__ void mma16816(float (&d)[4], const uint32_t (&a)[4], 
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-  __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<uint32_t*>(&v);
-}
-// GELU in its tanh form (Hendrycks & Gimpel 2016),
-//   gelu(x) = x/2 (1 + tanh(u)),  u = sqrt(2/pi) (x + 0.044715 x^3),
-// with tanh from the hardware tanh.approx.f32 instruction (one MUFU op; the
-// exact erf form costs ~20 instructions and dominated inference), and its
-// derivative 1/2 (1 + t) + x/2 (1 - t^2) sqrt(2/pi) (1 + 3 * 0.044715 x^2).
-__device__ __forceinline__ float tanh_approx(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float gelu(float z) {
-  const float u = 0.7978845608028654f * fmaf(0.044715f * z, z * z, z);
-  return 0.5f * z * (1.0f + tanh_approx(u));
-}
-__device__ __forceinline__ float gelu_grad(float z) {
-  const float z2 = z * z;
-  const float t = tanh_approx(0.7978845608028654f * fmaf(0.044715f * z, z2, z));
-  return 0.5f * (1.0f + t) + 0.5f * z * (1.0f - t * t) * 0.7978845608028654f * fmaf(0.134145f, z2, 1.0f);
-}
-
 // ---- generic bf16 GEMM with fused epilogues -------------------------------
 
 enum Epilogue { EPI_FWD_GELU = 0, EPI_FWD_LINEAR = 1, EPI_BWD_DGELU = 2, EPI_DW_ATOMIC = 3, EPI_STORE_F32 = 4 };
@@ -257,12 +232,6 @@ __global__ void adam_kernel(float* master, float* m, float* v, float* grad, bf16
 
 // ---- training inputs and targets --------------------------------------------
 
-// Network input of one sample: s / max, or log(max(s / max, 1e-6)) with log_in.
-__device__ __forceinline__ float input_transform(float s, float inv, int log_in) {
-  const float x = s * inv;
-  return log_in ? logf(fmaxf(x, 1e-6f)) : x;
-}
-
 // x_rows (n x ldx) bf16 = transformed signals per voxel, column nin = 1,
 // remaining padding 0; snorm[v] = the per-voxel maximum. signals are SoA (nin, n).
 __global__ void prepare_inputs_kernel(const float* signals, long long n, int nin, bf16* x_rows, long long ldx,
@@ -326,27 +295,36 @@ struct InferSmem {
   float b1[HID], b2[HID], b3[HID], b4[NOUT_PAD];
 };
 
-// acc (16 voxels x 128, 16 n8 tiles) + bias -> GELU -> bf16 A fragments (8 k16 tiles)
-__device__ __forceinline__ void act_to_afrag(const float (&acc)[16][4], const float* bias, int tq, uint32_t (&a)[8][4]) {
+// pre-activations (16 voxels x 128 in 16 n8 tiles, bias included) -> GELU ->
+// bf16 A fragments of the next layer (8 k16 tiles)
+__device__ __forceinline__ void act_to_afrag(const float (&acc)[16][4], uint32_t (&a)[8][4]) {
 #pragma unroll
   for (int kt = 0; kt < 8; ++kt) {
-    const int c0 = kt * 16 + 2 * tq, c1 = c0 + 8;
     const float* lo = acc[2 * kt];
     const float* hi = acc[2 * kt + 1];
-    a[kt][0] = pack_bf16(gelu(lo[0] + bias[c0]), gelu(lo[1] + bias[c0 + 1]));
-    a[kt][1] = pack_bf16(gelu(lo[2] + bias[c0]), gelu(lo[3] + bias[c0 + 1]));
-    a[kt][2] = pack_bf16(gelu(hi[0] + bias[c1]), gelu(hi[1] + bias[c1 + 1]));
-    a[kt][3] = pack_bf16(gelu(hi[2] + bias[c1]), gelu(hi[3] + bias[c1 + 1]));
+    a[kt][0] = pack_bf16(gelu(lo[0]), gelu(lo[1]));
+    a[kt][1] = pack_bf16(gelu(lo[2]), gelu(lo[3]));
+    a[kt][2] = pack_bf16(gelu(hi[0]), gelu(hi[1]));
+    a[kt][3] = pack_bf16(gelu(hi[2]), gelu(hi[3]));
+  }
+}
+
+// accumulators start at the layer's bias (column 2t, 2t+1 of each n8 tile)
+__device__ __forceinline__ void bias_init(float (&acc)[16][4], const float* bias, int tq) {
+#pragma unroll
+  for (int nt = 0; nt < 16; ++nt) {
+    const float b0 = bias[nt * 8 + 2 * tq], b1 = bias[nt * 8 + 2 * tq + 1];
+    acc[nt][0] = b0;
+    acc[nt][1] = b1;
+    acc[nt][2] = b0;
+    acc[nt][3] = b1;
   }
 }
 
 template <int NIN>
-__device__ __forceinline__ void hidden_layer(const bf16 (*w)[LDH], const uint32_t (&a)[8][4], float (&acc)[16][4],
-                                             int lane) {
-#pragma unroll
-  for (int nt = 0; nt < 16; ++nt)
-#pragma unroll
-    for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
+__device__ __forceinline__ void hidden_layer(const bf16 (*w)[LDH], const float* bias, const uint32_t (&a)[8][4],
+                                             float (&acc)[16][4], int lane) {
+  bias_init(acc, bias, lane & 3);
 #pragma unroll
   for (int kt = 0; kt < 8; ++kt)
 #pragma unroll
@@ -359,7 +337,7 @@ __device__ __forceinline__ void hidden_layer(const bf16 (*w)[LDH], const uint32_
 }
 
 template <int NIN>
-__global__ void __launch_bounds__(256) mlp_infer_kernel(const InferArgs p) {
+__global__ void __launch_bounds__(384, 1) mlp_infer_kernel(const InferArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& S = *reinterpret_cast<InferSmem<NIN>*>(smem_raw);
   // stage weights and biases
@@ -412,10 +390,7 @@ __global__ void __launch_bounds__(256) mlp_infer_kernel(const InferArgs p) {
     m1 = fmaxf(m1, 1e-20f);
     const float i0 = 1.f / m0, i1 = 1.f / m1;
     float acc[16][4];
-#pragma unroll
-    for (int nt = 0; nt < 16; ++nt)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc[nt][e] = 0.f;
+    bias_init(acc, S.b1, tq);
 #pragma unroll
     for (int kt = 0; kt < KT1; ++kt) {
       uint32_t a[4];
@@ -433,11 +408,11 @@ __global__ void __launch_bounds__(256) mlp_infer_kernel(const InferArgs p) {
       }
     }
     uint32_t af[8][4];
-    act_to_afrag(acc, S.b1, tq, af);
-    hidden_layer<NIN>(S.w2, af, acc, lane);
-    act_to_afrag(acc, S.b2, tq, af);
-    hidden_layer<NIN>(S.w3, af, acc, lane);
-    act_to_afrag(acc, S.b3, tq, af);
+    act_to_afrag(acc, af);
+    hidden_layer<NIN>(S.w2, S.b2, af, acc, lane);
+    act_to_afrag(acc, af);
+    hidden_layer<NIN>(S.w3, S.b3, af, acc, lane);
+    act_to_afrag(acc, af);
     float y[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int kt = 0; kt < 8; ++kt) {
@@ -586,9 +561,9 @@ int pcgb_mlp_forward(const float* signals, int64_t n, int nin, int log_in, const
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long long tiles = (n + 15) / 16;
-  long long blocks = (tiles + 7) / 8;
-  if (blocks > 2LL * sms) blocks = 2LL * sms;
-  mlp_infer_kernel<16><<<unsigned(blocks), 256, smem, static_cast<cudaStream_t>(stream)>>>(a);
+  long long blocks = (tiles + 11) / 12;
+  if (blocks > sms) blocks = sms;
+  mlp_infer_kernel<16><<<unsigned(blocks), 384, smem, static_cast<cudaStream_t>(stream)>>>(a);
   e = cudaGetLastError();
   return e == cudaSuccess ? PCGB_OK : mlp_fail(PCGB_ECUDA, cudaGetErrorString(e));
 }

@@ -1,0 +1,405 @@
+// Warm-start network inference on the 5th-generation tensor cores (tcgen05).
+//
+// Same network and numerics as mlp_infer_kernel in mlp.cu (16 -> 128 -> 128
+// -> 128 -> P, GELU, bf16 operands, fp32 accumulation; the bf16 roundings
+// happen at the same points), restructured for sm_103a:
+//
+//   * one CTA per SM, 16 warps = 4 warpgroups; each warpgroup owns one
+//     128-voxel tile at a time (thread t of the warpgroup = voxel t = TMEM
+//     lane t) and its own 128 TMEM columns for the layer accumulator;
+//   * a layer is D[128 x N] = A[128 x K] * W^T with A (activations) and W
+//     (weights, N x K) in shared memory, issued as K/16 tcgen05.mma
+//     (kind::f16, bf16 x bf16 -> f32, M = 128) by one thread of the
+//     warpgroup and tracked by tcgen05.commit on the warpgroup's mbarrier;
+//   * the epilogue of a layer reads the accumulator row of its voxel from
+//     TMEM (tcgen05.ld 32x32b), adds the bias, applies GELU and writes the
+//     bf16 row as the next layer's A operand back into shared memory;
+//   * the four warpgroups run independent tiles, so one warpgroup's MMAs
+//     overlap the other warpgroups' epilogues.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8 x 16-byte core matrices (8 rows x 8 bf16), element (r, k) of an R x K
+// operand at byte (r / 8) * SBO + (k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2
+// with LBO = 128 (next core matrix along K) and SBO = K / 8 * 128 (next
+// 8-row group). Every wait on an mbarrier is bounded: on timeout the kernel
+// records an error in *status, stops issuing work and still frees its TMEM.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "mlp_math.cuh"
+#include "pcgb.h"
+
+namespace pcgb_mlp_tc {
+
+using pcgb_mlp::bf16;
+
+constexpr int NIN = 16;
+constexpr int HID = 128;
+constexpr int NOUT_MMA = 16;  // the last layer's N (>= P, multiple of 16)
+constexpr int NOUT_MAX = 8;
+constexpr int NWG = 4;        // warpgroups (tiles in flight) per CTA
+constexpr int THREADS = NWG * 128;
+constexpr int TMEM_COLS = 512;  // NWG x 128 accumulator columns
+constexpr int LDH_G = HID + 8;  // leading dimension of the hidden weights in global memory
+constexpr int LD1_G = NIN + 8;  // ... of the first layer's weights
+constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait counts as lost
+
+struct __align__(1024) TcSmem {
+  bf16 w1[HID * NIN];
+  bf16 w2[HID * HID];
+  bf16 w3[HID * HID];
+  bf16 w4[NOUT_MMA * HID];
+  bf16 x[NWG][128 * NIN];
+  bf16 act[NWG][128 * HID];
+  float b1[HID], b2[HID], b3[HID], b4[NOUT_MMA];
+  unsigned long long mbar[NWG];
+  uint32_t tmem_base;
+};
+
+struct TcArgs {
+  const float* signals;  // SoA (NIN, n)
+  long long n;
+  const bf16* w[4];      // bf16 weights, rows x (in + 8)
+  const float* mw[4];    // fp32 master copies; column `in` holds the bias
+  int nout;
+  int log_in;
+  int kinds[NOUT_MAX];
+  float mean[NOUT_MAX], stdv[NOUT_MAX], lb[NOUT_MAX], ub[NOUT_MAX];
+  float* out;            // SoA (nout, n)
+  int* status;           // 0 = ok, else the kernel lost an mbarrier wait (may be null)
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// byte offset of element (r, k) of an R x K operand in the core-matrix layout
+__device__ __forceinline__ uint32_t core_off(int r, int k, int K) {
+  return uint32_t((r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start, LBO, SBO (bytes, multiples of 16),
+// descriptor version 1 (bits 46-47), no swizzle (bits 61-63 = 0)
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return uint64_t((addr >> 4) & 0x3FFFu) | (uint64_t((lbo >> 4) & 0x3FFFu) << 16) |
+         (uint64_t((sbo >> 4) & 0x3FFFu) << 32) | (uint64_t(1) << 46);
+}
+
+// instruction descriptor of kind::f16: D f32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9 and 10-12 = 1), both K-major, N >> 3 at bits 17-22, M >> 4 at 24-28
+__host__ __device__ constexpr uint32_t idesc_bf16(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(n >> 3) << 17) | (uint32_t(m >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
+}
+__device__ __forceinline__ void fence_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void wg_sync(int g) { asm volatile("bar.sync %0, 128;" ::"r"(g + 1) : "memory"); }
+// warpgroup barrier that also returns whether any thread passed `lost`
+__device__ __forceinline__ bool wg_sync_any(int g, bool lost) {
+  uint32_t r;
+  asm volatile(
+      "{\n.reg .pred p, q;\nsetp.ne.u32 q, %1, 0;\nbar.red.or.pred p, %2, 128, q;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(r)
+      : "r"(uint32_t(lost)), "r"(g + 1)
+      : "memory");
+  return r != 0;
+}
+
+// bounded wait for the phase `parity` of an mbarrier; false if it never completed
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (unsigned i = 0; i < kWaitLimit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// 32 consecutive fp32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
+      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// copy a rows x cols bf16 matrix (global leading dimension ldg) into the
+// core-matrix layout with K = kdim (columns >= cols and rows >= rows_live are zero)
+__device__ void stage_weights(bf16* dst, const bf16* src, int rows, int rows_live, int kdim, int ldg) {
+  const int chunks = rows * (kdim / 8);
+  unsigned char* base = reinterpret_cast<unsigned char*>(dst);
+  for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
+    const int r = c / (kdim / 8), k = (c % (kdim / 8)) * 8;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (r < rows_live) v = *reinterpret_cast<const uint4*>(src + (long long)r * ldg + k);
+    *reinterpret_cast<uint4*>(base + core_off(r, k, kdim)) = v;
+  }
+}
+
+// bias + GELU of 32 accumulator columns [c0, c0 + 32), written as bf16 into
+// row r of the next layer's A operand
+__device__ __forceinline__ void gelu_row_chunk(const float (&acc)[32], const float* bias, int c0, bf16* act, int r) {
+  unsigned char* base = reinterpret_cast<unsigned char*>(act);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    uint4 o;
+    uint32_t* w = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int j = q * 8 + 2 * e;
+      w[e] = pcgb_mlp::pack_bf16(pcgb_mlp::gelu(acc[j] + bias[c0 + j]), pcgb_mlp::gelu(acc[j + 1] + bias[c0 + j + 1]));
+    }
+    *reinterpret_cast<uint4*>(base + core_off(r, c0 + q * 8, HID)) = o;
+  }
+}
+
+__global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = warp >> 2;                   // warpgroup
+  const int r = (warp & 3) * 32 + lane;      // voxel row of the tile = TMEM lane
+
+  // weights, biases, barriers, TMEM
+  stage_weights(S.w1, p.w[0], HID, HID, NIN, LD1_G);
+  stage_weights(S.w2, p.w[1], HID, HID, HID, LDH_G);
+  stage_weights(S.w3, p.w[2], HID, HID, HID, LDH_G);
+  stage_weights(S.w4, p.w[3], NOUT_MMA, NOUT_MAX, HID, LDH_G);
+  for (int i = threadIdx.x; i < HID; i += blockDim.x) {
+    S.b1[i] = p.mw[0][i * LD1_G + NIN];
+    S.b2[i] = p.mw[1][i * LDH_G + HID];
+    S.b3[i] = p.mw[2][i * LDH_G + HID];
+  }
+  if (threadIdx.x < NOUT_MMA) S.b4[threadIdx.x] = threadIdx.x < NOUT_MAX ? p.mw[3][threadIdx.x * LDH_G + HID] : 0.f;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NWG; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.mbar[i])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_async_smem();  // staged weights -> visible to the tensor cores
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+
+  const uint32_t tbase = S.tmem_base;
+  const uint32_t d_tmem = tbase + uint32_t(g * 128);                           // lane 0, this warpgroup's columns
+  const uint32_t t_row = tbase + (uint32_t((warp & 3) * 32) << 16) + uint32_t(g * 128);  // this warp's lanes
+  const uint32_t mbar = smem_u32(&S.mbar[g]);
+  const uint32_t xs = smem_u32(S.x[g]), as = smem_u32(S.act[g]);
+  const uint32_t w1s = smem_u32(S.w1), w2s = smem_u32(S.w2), w3s = smem_u32(S.w3), w4s = smem_u32(S.w4);
+  const bool issuer = r == 0;
+  constexpr uint32_t ID_HID = idesc_bf16(128, HID), ID_OUT = idesc_bf16(128, NOUT_MMA);
+  uint32_t phase = 0;
+  bool lost = false;
+
+  const long long ntiles = (p.n + 127) / 128;
+  for (long long tile = (long long)blockIdx.x * NWG + g; tile < ntiles && !lost;
+       tile += (long long)gridDim.x * NWG) {
+    const long long v = tile * 128 + r;
+    // ---- inputs: 16 samples of voxel v -> bf16 row r of x
+    float s[NIN];
+    float mx = 0.f;
+#pragma unroll
+    for (int k = 0; k < NIN; ++k) {
+      s[k] = v < p.n ? p.signals[(long long)k * p.n + v] : 0.f;
+      mx = fmaxf(mx, s[k]);
+    }
+    mx = fmaxf(mx, 1e-20f);
+    const float inv = 1.f / mx;
+    {
+      unsigned char* xb = reinterpret_cast<unsigned char*>(S.x[g]);
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        uint4 o;
+        uint32_t* w = reinterpret_cast<uint32_t*>(&o);
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+          w[e] = pcgb_mlp::pack_bf16(pcgb_mlp::input_transform(s[q * 8 + 2 * e], inv, p.log_in),
+                                     pcgb_mlp::input_transform(s[q * 8 + 2 * e + 1], inv, p.log_in));
+        *reinterpret_cast<uint4*>(xb + core_off(r, q * 8, NIN)) = o;
+      }
+    }
+    // ---- four layers
+    for (int layer = 0; layer < 4; ++layer) {
+      fence_async_smem();   // this thread's A row -> visible to the tensor cores
+      fence_before_sync();  // its earlier TMEM reads are done
+      wg_sync(g);
+      if (issuer) {
+        fence_after_sync();
+        if (layer == 0) {
+          mma_bf16(d_tmem, smem_desc(xs, 128, 256), smem_desc(w1s, 128, 256), ID_HID, 0u);
+        } else {
+          const uint32_t ws = layer == 1 ? w2s : (layer == 2 ? w3s : w4s);
+          const uint32_t id = layer == 3 ? ID_OUT : ID_HID;
+#pragma unroll
+          for (int kk = 0; kk < HID / 16; ++kk)
+            mma_bf16(d_tmem, smem_desc(as + kk * 256, 128, 2048), smem_desc(ws + kk * 256, 128, 2048), id,
+                     kk > 0 ? 1u : 0u);
+        }
+        mma_commit(mbar);
+      }
+      const bool ok = mbar_wait(mbar, phase);
+      phase ^= 1u;
+      if (wg_sync_any(g, !ok)) {
+        lost = true;
+        break;
+      }
+      fence_after_sync();
+      if (layer < 3) {
+        const float* bias = layer == 0 ? S.b1 : (layer == 1 ? S.b2 : S.b3);
+#pragma unroll 1
+        for (int c = 0; c < HID / 32; ++c) {
+          float acc[32];
+          tmem_ld32(t_row + uint32_t(c * 32), acc);
+          gelu_row_chunk(acc, bias, c * 32, S.act[g], r);
+        }
+      } else {
+        float y[16];
+        tmem_ld16(t_row, y);
+        if (v < p.n) {
+#pragma unroll
+          for (int k = 0; k < NOUT_MAX; ++k) {
+            if (k >= p.nout) break;
+            const float t = (y[k] + S.b4[k]) * p.stdv[k] + p.mean[k];
+            const int kind = p.kinds[k];
+            float val = kind == 0 ? t * mx : (kind == 2 ? expf(t) : t);
+            val = fminf(fmaxf(val, p.lb[k]), p.ub[k]);
+            p.out[(long long)k * p.n + v] = val;
+          }
+        }
+      }
+    }
+  }
+  if (lost && issuer) {
+    // the lost phase may still complete: give the warpgroup's MMAs a second
+    // bounded wait before the TMEM they write is returned
+    (void)mbar_wait(mbar, phase ^ 1u);
+    if (p.status) atomicExch(p.status, 1);
+  }
+  // all TMEM reads done before the allocation is returned
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after_sync();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+thread_local std::string g_err;
+
+}  // namespace pcgb_mlp_tc
+
+using namespace pcgb_mlp_tc;
+
+extern "C" {
+
+const char* pcgb_mlp_tc_last_error(void) { return g_err.c_str(); }
+
+int pcgb_mlp_forward_tc(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
+                        const float* const* w_master, int nout, const int* kinds, const float* mean, const float* stdv,
+                        const float* lb, const float* ub, float* out, int* status, void* stream) {
+  g_err.clear();
+  if (n < 0) {
+    g_err = "n must be >= 0";
+    return PCGB_EINVAL;
+  }
+  if (nin != NIN) {
+    g_err = "the tensor-core forward is built for 16 inputs";
+    return PCGB_EINVAL;
+  }
+  if (nout < 1 || nout > NOUT_MAX) {
+    g_err = "nout must be 1..8";
+    return PCGB_EINVAL;
+  }
+  if (!w_bf16 || !w_master || !kinds || !mean || !stdv || !lb || !ub) {
+    g_err = "weights and output transforms are required";
+    return PCGB_EINVAL;
+  }
+  if (n == 0) return PCGB_OK;
+  if (!signals || !out) {
+    g_err = "signals and out are required";
+    return PCGB_EINVAL;
+  }
+  TcArgs a{};
+  a.signals = signals;
+  a.n = n;
+  for (int l = 0; l < 4; ++l) {
+    a.w[l] = static_cast<const bf16*>(w_bf16[l]);
+    a.mw[l] = w_master[l];
+  }
+  a.nout = nout;
+  a.log_in = log_in;
+  for (int k = 0; k < NOUT_MAX; ++k) {
+    a.kinds[k] = k < nout ? kinds[k] : 1;
+    a.mean[k] = k < nout ? mean[k] : 0.f;
+    a.stdv[k] = k < nout ? stdv[k] : 1.f;
+    a.lb[k] = k < nout ? lb[k] : -3.0e38f;
+    a.ub[k] = k < nout ? ub[k] : 3.0e38f;
+  }
+  a.out = out;
+  a.status = status;
+  const int smem = int(sizeof(TcSmem));
+  cudaError_t e = cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) {
+    g_err = cudaGetErrorString(e);
+    return PCGB_ECUDA;
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (sms < 1) sms = 1;
+  const long long tiles = (n + 127) / 128;
+  long long blocks = (tiles + NWG - 1) / NWG;
+  if (blocks > sms) blocks = sms;
+  mlp_infer_tc_kernel<<<unsigned(blocks), THREADS, smem, static_cast<cudaStream_t>(stream)>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_err = cudaGetErrorString(e);
+    return PCGB_ECUDA;
+  }
+  return PCGB_OK;
+}
+
+}  // extern "C"

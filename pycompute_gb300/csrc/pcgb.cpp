@@ -55,12 +55,15 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
 
 enum KernelSlot {
   K_LM_C1_B1, K_LM_C1_B0, K_LM_C0_B1, K_LM_C0_B0, K_COST_C1, K_COST_C0, K_GMW, K_EVAL_C1, K_EVAL_C0,
-  K_SEARCH_C1, K_SEARCH_C0, K_RS_C1_B1, K_RS_C1_B0, K_RS_C0_B1, K_RS_C0_B0, K_COUNT
+  K_SEARCH_C1, K_SEARCH_C0, K_RS_C1_B1, K_RS_C1_B0, K_RS_C0_B1, K_RS_C0_B0,
+  K_LMQ_C1_B1, K_LMQ_C1_B0, K_LMQ_C0_B1, K_LMQ_C0_B0, K_CHECK_C1, K_CHECK_C0, K_SELECT_C1, K_SELECT_C0, K_COUNT
 };
 const char* kKernelNames[K_COUNT] = {"pcgb_lm_c1_b1", "pcgb_lm_c1_b0", "pcgb_lm_c0_b1", "pcgb_lm_c0_b0",
                                      "pcgb_cost_c1",  "pcgb_cost_c0",  "pcgb_gmw81",    "pcgb_eval_c1",
                                      "pcgb_eval_c0",  "pcgb_search_c1", "pcgb_search_c0", "pcgb_rs_c1_b1",
-                                     "pcgb_rs_c1_b0", "pcgb_rs_c0_b1", "pcgb_rs_c0_b0"};
+                                     "pcgb_rs_c1_b0", "pcgb_rs_c0_b1", "pcgb_rs_c0_b0", "pcgb_lmq_c1_b1",
+                                     "pcgb_lmq_c1_b0", "pcgb_lmq_c0_b1", "pcgb_lmq_c0_b0", "pcgb_check_c1",
+                                     "pcgb_check_c0", "pcgb_select_c1", "pcgb_select_c0"};
 
 constexpr int kDefaultBlock = 128;
 constexpr int kMaxBlock = 256;
@@ -99,6 +102,11 @@ std::string program_source(const char* model_source, const char* model_struct, i
   s << "extern \"C\" __global__ void " << bounds << " pcgb_gmw81(const PcgbLmParams a) { pcgb::gmw81_grid<" << P
     << ", " << ts << ">(a); }\n";
   for (int c = 1; c >= 0; --c)
+    for (int b = 1; b >= 0; --b)
+      s << "extern \"C\" __global__ void " << bounds << " pcgb_lmq_c" << c << "_b" << b
+        << "(const PcgbLmParams a) { pcgb::lm_refill_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
+        << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
+  for (int c = 1; c >= 0; --c)
     s << "extern \"C\" __global__ void " << bounds << " pcgb_search_c" << c
       << "(const PcgbLmParams a) { pcgb::search_step_grid<PcgbModel, " << M << ", " << ta << ", "
       << (c ? "true" : "false") << ">(a); }\n";
@@ -107,6 +115,14 @@ std::string program_source(const char* model_source, const char* model_struct, i
       s << "extern \"C\" __global__ void " << bounds << " pcgb_rs_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::random_search_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
+  for (int c = 1; c >= 0; --c) {
+    s << "extern \"C\" __global__ void " << bounds << " pcgb_check_c" << c
+      << "(const PcgbLmParams a) { pcgb::warm_check_grid<PcgbModel, " << M << ", " << ta << ", "
+      << (c ? "true" : "false") << ">(a); }\n";
+    s << "extern \"C\" __global__ void " << bounds << " pcgb_select_c" << c
+      << "(const PcgbLmParams a) { pcgb::warm_select_grid<PcgbModel, " << M << ", " << ta << ", "
+      << (c ? "true" : "false") << ">(a); }\n";
+  }
   for (int c = 1; c >= 0; --c)
     s << "extern \"C\" __global__ void " << bounds << " pcgb_eval_c" << c
       << "(const PcgbLmParams a) { pcgb::eval_grid<PcgbModel, " << M << ", " << ta << ", " << (c ? "true" : "false")
@@ -524,7 +540,8 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
                        double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
                        void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
                        const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
-                       int block, const int32_t* vox_idx, int64_t n_items, void* stream) {
+                       int block, const int32_t* vox_idx, int64_t n_items, void* stream,
+                       uint32_t* work_counter = nullptr, int grid = 0, const uint32_t* n_items_dev = nullptr) {
   g_err.clear();
   if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
   if (nprobs < 0 || iters < 0) return fail(PCGB_EINVAL, "nprobs and iters must be >= 0");
@@ -568,6 +585,40 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
   prm.dec = dec;
   const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_LM_C1_B1 : K_LM_C1_B0)
                                              : (bounds_stride == 0 ? K_LM_C0_B1 : K_LM_C0_B0);
+  if (work_counter) {
+    // refill schedule: persistent grid, warps claim 256-item chunks from the counter
+    const KernelSlot q = KernelSlot(slot + (K_LMQ_C1_B1 - K_LM_C1_B1));
+    if (vox_idx) {
+      if (n_items < 0) return fail(PCGB_EINVAL, "n_items must be >= 0");
+      prm.vox_idx = vox_idx;
+      prm.n_items = n_items;
+    } else {
+      prm.n_items = nprobs;
+    }
+    if (prm.n_items == 0) return PCGB_OK;
+    if (prm.n_items / 256 >= (int64_t(1) << 31)) return fail(PCGB_ERANGE, "too many voxels for one refill launch");
+    prm.work = work_counter;
+    prm.n_items_dev = n_items_dev;
+    if (block <= 0) block = kDefaultBlock;
+    if (block > kMaxBlock || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to %d", kMaxBlock);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+    if (grid <= 0) {
+      int per_sm = 0, dev = 0, sms = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(ft->k[q]), block, 0);
+      if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+      grid = per_sm * sms;
+      const int64_t need = (prm.n_items + block - 1) / block;
+      if (grid > need) grid = int(need);
+    }
+    void* args[] = {&prm};
+    e = cudaLaunchKernel(reinterpret_cast<const void*>(ft->k[q]), dim3(grid), dim3(block), args, 0, st);
+    if (e != cudaSuccess) return cuda_fail(e, kKernelNames[q]);
+    return PCGB_OK;
+  }
   if (vox_idx) {
     if (n_items < 0) return fail(PCGB_EINVAL, "n_items must be >= 0");
     prm.vox_idx = vox_idx;
@@ -586,6 +637,117 @@ int pcgb_lm_run(pcgb_fitter* ft, const void* consts, int64_t consts_stride, cons
   return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
                      params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
                      protocol_len, lb_host, ub_host, block, nullptr, 0, stream);
+}
+
+int pcgb_lm_run_refill(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                       void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                       const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                       int block, const int32_t* vox_idx, int64_t n_items, const uint32_t* n_items_dev,
+                       uint32_t* work_counter, int grid, void* stream) {
+  g_err.clear();
+  if (!work_counter) return fail(PCGB_EINVAL, "work_counter is NULL");
+  if (n_items_dev && !vox_idx) return fail(PCGB_EINVAL, "n_items_dev needs vox_idx");
+  return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
+                     params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
+                     protocol_len, lb_host, ub_host, block, vox_idx, n_items, stream, work_counter, grid, n_items_dev);
+}
+
+int pcgb_warm_check(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                    const void* lower_bound, const void* upper_bound, int64_t bounds_stride,
+                    const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                    const double* init_values, double lam0, void* params, void* lam, int8_t* step_type, void* f,
+                    void* cost, void* pars_backup, void* cost_backup, int32_t* fb_idx, uint32_t* fb_count,
+                    int64_t nprobs, void* stream) {
+  g_err.clear();
+  if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
+  if (nprobs < 0) return fail(PCGB_EINVAL, "nprobs must be >= 0");
+  if (nprobs > (int64_t(1) << 31) - 1) return fail(PCGB_ERANGE, "warm check indexes voxels with int32");
+  if (!fb_count || !init_values) return fail(PCGB_EINVAL, "fb_count and init_values are required");
+  if (nprobs > 0 && (!data || !params || !lam || !step_type || !f || !cost || !pars_backup || !cost_backup || !fb_idx))
+    return fail(PCGB_EINVAL, "data, params, lam, step_type, f, cost, backups and fb_idx are required");
+  if (int rc = check_device(ft)) return rc;
+  PcgbLmParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  if (int rc = fill_protocol(ft, prm, consts_stride, nprobs, protocol_host, protocol_len)) return rc;
+  if (consts_stride != 0 && !consts) return fail(PCGB_EINVAL, "per-voxel consts pointer is NULL");
+  if (bounds_stride == 0) {
+    if (!lb_host || !ub_host) return fail(PCGB_EINVAL, "shared bounds need lb_host and ub_host");
+    for (int k = 0; k < ft->P; ++k) {
+      prm.shared_lb_d[k] = lb_host[k];
+      prm.shared_ub_d[k] = ub_host[k];
+      prm.shared_lb_f[k] = float(lb_host[k]);
+      prm.shared_ub_f[k] = float(ub_host[k]);
+    }
+  } else if (bounds_stride != nprobs || !lower_bound || !upper_bound) {
+    return fail(PCGB_EINVAL, "bounds_stride must be 0 (shared) or nprobs with device bounds");
+  }
+  for (int k = 0; k < ft->P; ++k) prm.init_val[k] = float(init_values[k]);
+  prm.pars = params;
+  prm.consts = consts;
+  prm.data = data;
+  prm.lb = lower_bound;
+  prm.ub = upper_bound;
+  prm.bstride = bounds_stride;
+  prm.lam = lam;
+  prm.step_type = reinterpret_cast<signed char*>(step_type);
+  prm.f = f;
+  prm.cost = cost;
+  prm.pars_backup = pars_backup;
+  prm.cost_backup = cost_backup;
+  prm.fb_idx = fb_idx;
+  prm.fb_count = fb_count;
+  prm.lam0 = lam0;
+  prm.N = nprobs;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(fb_count, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  return launch(ft, consts_stride == 0 ? K_CHECK_C1 : K_CHECK_C0, prm, nprobs, 256, stream);
+}
+
+int pcgb_warm_select(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                     const double* protocol_host, int protocol_len, void* params, void* cost, const void* pars_backup,
+                     const void* cost_backup, const int32_t* fb_idx, uint32_t* fb_count, int8_t* which,
+                     int64_t nprobs, void* stream) {
+  g_err.clear();
+  if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
+  if (nprobs < 0) return fail(PCGB_EINVAL, "nprobs must be >= 0");
+  if (!fb_count) return fail(PCGB_EINVAL, "fb_count is required");
+  if (nprobs > 0 && (!data || !params || !cost || !pars_backup || !cost_backup || !fb_idx))
+    return fail(PCGB_EINVAL, "data, params, cost, backups and fb_idx are required");
+  if (int rc = check_device(ft)) return rc;
+  if (nprobs == 0) return PCGB_OK;
+  PcgbLmParams prm;
+  std::memset(&prm, 0, sizeof(prm));
+  if (int rc = fill_protocol(ft, prm, consts_stride, nprobs, protocol_host, protocol_len)) return rc;
+  if (consts_stride != 0 && !consts) return fail(PCGB_EINVAL, "per-voxel consts pointer is NULL");
+  prm.pars = params;
+  prm.consts = consts;
+  prm.data = data;
+  prm.cost = cost;
+  prm.pars_backup = const_cast<void*>(pars_backup);
+  prm.cost_backup = const_cast<void*>(cost_backup);
+  prm.fb_idx = const_cast<int*>(fb_idx);
+  prm.fb_count = fb_count;
+  prm.n_items_dev = fb_count;
+  prm.n_items = nprobs;
+  prm.which = reinterpret_cast<signed char*>(which);
+  prm.N = nprobs;
+  const KernelSlot slot = consts_stride == 0 ? K_SELECT_C1 : K_SELECT_C0;
+  if (!ft->k[slot]) return fail(PCGB_EINVAL, "kernel %s missing from program", kKernelNames[slot]);
+  // the flagged count is known only on the device: a grid of 8 blocks per SM strides over it
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  int grid = 8 * (sms > 0 ? sms : 1);
+  const int64_t need = (nprobs + 255) / 256;
+  if (grid > need) grid = int(need);
+  void* args[] = {&prm};
+  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(ft->k[slot]), dim3(grid), dim3(256), args, 0,
+                                   static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, kKernelNames[slot]);
+  return PCGB_OK;
 }
 
 int pcgb_lm_run_subset(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,

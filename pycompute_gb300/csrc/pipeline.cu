@@ -11,9 +11,17 @@
 #include <string>
 
 #include "lm_params.h"
+#include "lm_kernel.cuh"
 #include "pcgb.h"
 
 namespace pcgb_pipe {
+
+// The FP64 reciprocal used by the FP64 GMW81 solve, applied elementwise so it
+// can be checked against a correctly rounded 1/x.
+__global__ void rcp64_kernel(const double* x, double* y, long long n) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = pcgb::rcp64(x[i]);
+}
 
 thread_local std::string g_err;
 int fail(int code, const char* m) {
@@ -244,6 +252,15 @@ using namespace pcgb_pipe;
 extern "C" {
 
 const char* pcgb_pipeline_last_error(void) { return g_err.c_str(); }
+
+int pcgb_rcp64(const double* x, double* y, int64_t n, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !y))) return fail(PCGB_EINVAL, "bad rcp64 arguments");
+  if (n == 0) return PCGB_OK;
+  const long long blocks = (n + 255) / 256;
+  if (blocks > 0x7fffffffLL) return fail(PCGB_ERANGE, "rcp64: n too large");
+  rcp64_kernel<<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, y, n);
+  return cuda_rc();
+}
 
 int pcgb_init_constant(const float* data, int64_t n, int m, int nparam, const double* values, float* pars,
                        void* stream) {

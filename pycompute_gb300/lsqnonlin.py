@@ -310,10 +310,21 @@ class SecondOrderLevenbergMarquardt:
         with torch.cuda.device(dev):
             self.build()
 
-    def run(self, iters: int, tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0, block: int = 0):
-        """Run ``iters`` iterations on every voxel (lsqnonlin.py:1058-1073). Asynchronous; returns None."""
+    def run(self, iters: int, tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0, block: int = 0,
+            schedule: str = "grid"):
+        """Run ``iters`` iterations on every voxel (lsqnonlin.py:1058-1073). Asynchronous; returns None.
+
+        ``schedule="grid"`` gives each thread one voxel for the whole fit;
+        ``schedule="refill"`` runs a persistent grid whose warps hand a new
+        voxel to any lane whose voxel has converged (same results, fewer idle
+        lanes when convergence is ragged).
+        """
         if not hasattr(self, "pars_t"):
             raise RuntimeError("setup() must be called before run()")
+        if schedule == "refill":
+            return self._run_refill(iters, tol, mu, eta, acc, dec, block, None, 0)
+        if schedule != "grid":
+            raise ValueError("schedule must be 'grid' or 'refill'")
         with torch.cuda.device(self.pars_t.device):
             prog = self.build()
             L = _lib.lib()
@@ -329,6 +340,25 @@ class SecondOrderLevenbergMarquardt:
                                len(self._protocol or []), lbh if self._bstride == 0 else None,
                                ubh if self._bstride == 0 else None, int(block), ctypes.c_void_p(_stream_ptr()))
             _lib.check("pcgb_lm_run", rc)
+        return None
+
+    def _run_refill(self, iters, tol, mu, eta, acc, dec, block, vox_idx, n_items, grid: int = 0, n_items_dev=None):
+        with torch.cuda.device(self.pars_t.device):
+            prog = self.build()
+            if getattr(self, "_counter", None) is None or self._counter.device != self.pars_t.device:
+                self._counter = torch.zeros(1, dtype=torch.int32, device=self.pars_t.device)
+            pv, plen = self._proto_args()
+            lbh = (ctypes.c_double * self.nparam)(*(self._lb_host or [0.0] * self.nparam))
+            ubh = (ctypes.c_double * self.nparam)(*(self._ub_host or [0.0] * self.nparam))
+            rc = _lib.lib().pcgb_lm_run_refill(
+                prog.handle, _ptr(self.consts_t), self._cstride, _ptr(self.data_t), _ptr(self.lower_bound_t),
+                _ptr(self.upper_bound_t), self._bstride, float(tol), float(mu), float(eta), float(acc), float(dec),
+                _ptr(self.pars_t), _ptr(self.step_t), _ptr(self.lam_t), _ptr(self.step_type_t), _ptr(self.f_t),
+                _ptr(self.first_f), _ptr(self.last_f), _ptr(self.iters_t), self.Nprobs, int(iters), pv, plen,
+                lbh if self._bstride == 0 else None, ubh if self._bstride == 0 else None, int(block),
+                _ptr(vox_idx) if vox_idx is not None else None, int(n_items), _ptr(n_items_dev),
+                _ptr(self._counter), int(grid), ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_lm_run_refill", rc)
         return None
 
 
@@ -357,8 +387,12 @@ class SecondOrderLevenbergMarquardt:
         return out
 
     def run_subset(self, vox_idx: torch.Tensor, n_items: int, iters: int, tol=1e-8, mu=0.25, eta=0.75, acc=0.2,
-                   dec=2.0, block: int = 0):
+                   dec=2.0, block: int = 0, schedule: str = "grid"):
         """run() restricted to the voxels listed in ``vox_idx`` (int32, first n_items entries)."""
+        if schedule == "refill":
+            return self._run_refill(iters, tol, mu, eta, acc, dec, block, vox_idx, n_items)
+        if schedule != "grid":
+            raise ValueError("schedule must be 'grid' or 'refill'")
         with torch.cuda.device(self.pars_t.device):
             prog = self.build()
             pv, plen = self._proto_args()

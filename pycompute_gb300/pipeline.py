@@ -100,8 +100,27 @@ class WarmStartFitter:
         w = self.w
         return list(w.protocol), list(w.lb), list(w.ub)
 
+    def _buffers(self, P: int, N: int, dev):
+        key = (P, N, str(dev))
+        if getattr(self, "_buf_key", None) != key:
+            self._buf = dict(cost=torch.empty(N, dtype=torch.float32, device=dev),
+                             backup=torch.empty((P, N), dtype=torch.float32, device=dev),
+                             cost_b=torch.empty(N, dtype=torch.float32, device=dev),
+                             idx=torch.empty(N, dtype=torch.int32, device=dev),
+                             counts=torch.zeros(2, dtype=torch.int32, device=dev))
+            self._buf_key = key
+        return self._buf
+
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
-            lam0: float = 1e-3, timings: dict | None = None):
+            lam0: float = 1e-3, timings: dict | None = None, fused: bool = True):
+        """Warm-started fit of data (M, N); returns a WarmFit.
+
+        ``fused`` (default) runs steps 3-5 as three kernels that never return
+        the flagged count to the host (check + compaction + state reset in one
+        pass; the refit takes the count from device memory; cost + select in
+        one pass); ``fused=False`` runs them as the separate pipeline kernels
+        (cost, constant start, cost, flags, prepare, refit, cost, select).
+        """
         w = self.w
         dev = data.device
         M, N = data.shape
@@ -124,6 +143,31 @@ class WarmStartFitter:
         mark("setup")
         solm.run(iters_warm)
         mark("lm_warm")
+        if fused:
+            b = self._buffers(P, N, dev)
+            L = _lib.lib()
+            prog = solm.build()
+            pv, plen = solm._proto_args()
+            rc = L.pcgb_warm_check(prog.handle, _p(solm.consts_t), solm._cstride, _p(data), _p(solm.lower_bound_t),
+                                   _p(solm.upper_bound_t), solm._bstride, pv, plen,
+                                   _dvec(solm._lb_host) if solm._bstride == 0 else None,
+                                   _dvec(solm._ub_host) if solm._bstride == 0 else None, _dvec(w.init_values), 5.0,
+                                   _p(pars), _p(solm.lam_t), _p(solm.step_type_t), _p(solm.f_t), _p(b["cost"]),
+                                   _p(b["backup"]), _p(b["cost_b"]), _p(b["idx"]), _p(b["counts"]), N, _stream())
+            _lib.check("pcgb_warm_check", rc)
+            mark("check")
+            solm._run_refill(iters_fallback, 1e-8, 0.25, 0.75, 0.2, 2.0, 0, b["idx"], N, n_items_dev=b["counts"])
+            mark("refit")
+            rc = L.pcgb_warm_select(prog.handle, _p(solm.consts_t), solm._cstride, _p(data), pv, plen, _p(pars),
+                                    _p(b["cost"]), _p(b["backup"]), _p(b["cost_b"]), _p(b["idx"]), _p(b["counts"]),
+                                    None, N, _stream())
+            _lib.check("pcgb_warm_select", rc)
+            mark("select")
+            if timings is not None:
+                torch.cuda.synchronize()
+                for (n0, e0), (n1, e1) in zip(ev[:-1], ev[1:]):
+                    timings[n1] = timings.get(n1, 0.0) + e0.elapsed_time(e1)
+            return WarmFit(pars, b["cost"], b["counts"], solm.step_type_t)
         cost = solm.cost()
         # cost at the plain fitter's starting point
         p0 = init_constant(data, w.init_values)
@@ -158,7 +202,26 @@ class WarmStartFitter:
             torch.cuda.synchronize()
             for (n0, e0), (n1, e1) in zip(ev[:-1], ev[1:]):
                 timings[n1] = timings.get(n1, 0.0) + e0.elapsed_time(e1)
-        return dict(pars=pars, cost=cost, n_fallback=nfb, n_refit_kept=kept_refit, step_type=solm.step_type_t)
+        return WarmFit(pars, cost, torch.tensor([nfb, kept_refit], dtype=torch.int32), solm.step_type_t)
+
+
+class WarmFit:
+    """Result of WarmStartFitter.fit: pars (P, N), cost (N), step_type (1, N)
+    on the device; n_fallback / n_refit_kept read the device counters (a sync)."""
+
+    def __init__(self, pars, cost, counts, step_type):
+        self.pars, self.cost, self.counts, self.step_type = pars, cost, counts, step_type
+
+    @property
+    def n_fallback(self) -> int:
+        return int(self.counts[0].item())
+
+    @property
+    def n_refit_kept(self) -> int:
+        return int(self.counts[1].item())
+
+    def __getitem__(self, key):
+        return getattr(self, key)
 
 
 def bpolyfit(y: torch.Tensor, deg: int, x_shared=None, x: torch.Tensor | None = None, row0: int = 0,

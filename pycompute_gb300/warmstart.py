@@ -256,8 +256,13 @@ class WarmStartMLP:
         return self
 
     # ---- inference ------------------------------------------------------------
-    def infer(self, signals: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
-        """Initial parameters (nout, n) for signals (nin, n)."""
+    def infer(self, signals: torch.Tensor, out: torch.Tensor | None = None, impl: str = "tcgen05") -> torch.Tensor:
+        """Initial parameters (nout, n) for signals (nin, n).
+
+        ``impl="tcgen05"`` (default) runs the tensor-memory kernel,
+        ``impl="mma"`` the warp-level mma.sync kernel; both compute the same
+        network with the same bf16 roundings.
+        """
         n = signals.shape[1]
         if out is None:
             out = torch.empty((self.nout, n), dtype=torch.float32, device=signals.device)
@@ -266,8 +271,23 @@ class WarmStartMLP:
         kinds = (ctypes.c_int * self.nout)(*self.kinds)
         fl = lambda v: (ctypes.c_float * self.nout)(*[float(x) for x in v])  # noqa: E731
         with torch.cuda.device(signals.device):
-            rc = _lib.lib().pcgb_mlp_forward(_p(signals), n, self.nin, int(self.log_in), wb, wm, self.nout, kinds,
-                                             fl(self.mean),
-                                             fl(self.std), fl(self.lb), fl(self.ub), _p(out), _stream())
-        _lib.check("pcgb_mlp_forward", rc)
+            if impl == "tcgen05":
+                if getattr(self, "_status", None) is None or self._status.device != signals.device:
+                    self._status = torch.zeros(1, dtype=torch.int32, device=signals.device)
+                rc = _lib.lib().pcgb_mlp_forward_tc(_p(signals), n, self.nin, int(self.log_in), wb, wm, self.nout,
+                                                    kinds, fl(self.mean), fl(self.std), fl(self.lb), fl(self.ub),
+                                                    _p(out), _p(self._status), _stream())
+                _lib.check("pcgb_mlp_forward_tc", rc)
+            elif impl == "mma":
+                rc = _lib.lib().pcgb_mlp_forward(_p(signals), n, self.nin, int(self.log_in), wb, wm, self.nout,
+                                                 kinds, fl(self.mean), fl(self.std), fl(self.lb), fl(self.ub),
+                                                 _p(out), _stream())
+                _lib.check("pcgb_mlp_forward", rc)
+            else:
+                raise ValueError("impl must be 'tcgen05' or 'mma'")
         return out
+
+    def tc_status(self) -> int:
+        """Nonzero if a tcgen05 inference gave up on a bounded wait (reads the device flag)."""
+        st = getattr(self, "_status", None)
+        return 0 if st is None else int(st.item())

@@ -83,6 +83,31 @@ def test_fallback_refits_flagged_voxels():
     assert np.all(cost[refit] <= c_plain.cpu().numpy()[refit] * (1 + 1e-6) + 1e-3)
 
 
+@pytest.mark.parametrize("per_voxel_bounds", [False, True])
+def test_fused_fallback_matches_separate_kernels(per_voxel_bounds):
+    """Check + refit + select as three fused kernels (no host read of the
+    flagged count) give the same fits, costs and counts as the separate
+    pipeline kernels."""
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    _, data = pipeline.synth_gpu(w, 50001, seed=7, device=DEV)
+    out = []
+    for fused in (False, True):
+        wf = pipeline.WarmStartFitter(w, _BadNet(w))
+        if per_voxel_bounds:
+            N = data.shape[1]
+            lbt = torch.tensor(w.lb, device=DEV)[:, None].expand(w.P, N).contiguous()
+            ubt = torch.tensor(w.ub, device=DEV)[:, None].expand(w.P, N).contiguous()
+            wf._consts = lambda dev, lbt=lbt, ubt=ubt: (list(w.protocol), lbt, ubt)
+        res = wf.fit(data, iters_warm=3, iters_fallback=20, fused=fused)
+        torch.cuda.synchronize()
+        out.append((res.pars.cpu().numpy().copy(), res.cost.cpu().numpy().copy(), res.n_fallback, res.n_refit_kept))
+    (p0, c0, n0, k0), (p1, c1, n1, k1) = out
+    assert n0 == n1 and n0 >= 16667
+    assert k0 == k1
+    np.testing.assert_array_equal(p0, p1)
+    np.testing.assert_array_equal(c0, c1)
+
+
 def test_trained_network_beats_plain_lm_at_equal_iterations():
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     # training set: signals and the plain LM's fits of them as labels
