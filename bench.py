@@ -1,33 +1,47 @@
-"""Benchmark: IVIM voxel fits/s of the batched LM fitter on GB300.
+"""Benchmark: IVIM voxel fits/s at 1e-4 relative error vs FP64, MLP warm start
+vs plain LM, on GB300.
 
-Workload (default): plain LM at scale - IVIM bi-exponential, 4 parameters,
-b = {0,10,20,50,100,200,400,600,800,1000} s/mm^2, 256x256x128 = 8,388,608
-voxels, fp32 state with the GMW81 solve and gain-ratio test in fp64, at most
-100 iterations per voxel, constant initialisation [max S, 0.1, 1e-2, 1e-3],
-seeded synthetic signals (uniform true parameters, Rician noise at SNR 50).
+Headline workload: IVIM bi-exponential, 4 parameters, 16 b-values (0-1000
+s/mm^2, log-spaced above 10), 16,777,216 voxels, seeded synthetic signals
+(uniform true parameters S0 in [500, 1500], f in [0.05, 0.35], D* in
+[5e-3, 5e-2], D in [0.5e-3, 2.5e-3], Rician noise sigma = S0/50), fp32 state
+with the GMW81 solve and gain-ratio test in fp64.
 
-One step = one full fit of every voxel: the fitter state is reset from the
-initial parameters and run(100) is called. Inputs (335 MB of signals) are
-larger than L2 (129 MB), so no L2 flush is needed between steps.
+Untimed setup: the warm-start network (16 -> 128 -> 128 -> 128 -> 4, GELU,
+bf16 weights, fp32 accumulation) is trained on 2,097,152 other synthetic
+signals with the plain LM's converged fits as labels; the all-FP64 fit (same
+LM, constant start, 300 iterations, tolerance 1e-30) of the evaluation voxels
+is the error reference; for each method the iteration budget is the smallest
+whose median relative error (per voxel the worst parameter) is <= 1e-4.
+
+One step = one fit of every voxel at that budget:
+  warm start   network -> LM (k_warm iterations from lambda 3e-3) -> fused
+               fallback check -> plain-LM refit of flagged voxels on a device
+               list -> keep the lower cost (WarmStartFitter.fit)
+  plain LM     constant start -> LM (k_plain iterations), reported beside it
+Inputs (1.07 GB of signals) are larger than L2 (129 MB): no flush needed.
 
 Reported (one JSON line from rank 0):
-  value        fits/s with inputs resident in HBM (whole job over ranks)
-  e2e          fits/s through the public API from pinned host buffers,
-               host->device copies of signals and initial parameters and the
-               device->host read of fitted parameters and status inside the
-               timed region
-  roofline     HBM roofline of the LM kernel: algorithmic bytes
-               (4M + 4P + 1 per voxel: signals in, parameters and status out)
-               over the kernel's event-timed duration, against the measured
-               copy bandwidth in MEASURED_PEAKS.json
-  cpu_baseline the CPU oracle (the reference algorithm in fp32) on a bounded
-               sample on all host cores
-  accuracy     median relative error of the fitted maps against the all-FP64
-               GPU fitter (same LM, same initialisation)
+  value         warm-start fits/s with inputs resident in HBM (whole job)
+  plain_lm      plain-LM fits/s at its own 1e-4 budget, and the speedup
+  e2e           warm-start fits/s through the public API: signals copied
+                from pinned host memory and the fitted parameters copied
+                back inside the timed region
+  roofline      the LM kernel of the warm step (the dominant kernel):
+                algorithmic bytes 4M + 8P + 1 per voxel (signals in,
+                parameters in and out, status) over its event-timed duration,
+                against the measured copy bandwidth; roofline_network the
+                tensor-core network kernel against measured bf16 throughput
+  cpu_baseline  the reference algorithm (plain LM, fp32) on the host cores at
+                its own 1e-4 budget on a bounded IVIM-16 sample
+  plain_lm_ivim10_8.4M  the plain LM at scale (IVIM-10, 8,388,608 voxels,
+                100 iterations) with its accuracy against the FP64 fitter
+  mixed_batch   four models in one persistent launch vs one launch per model
 
-`--impl reference` times the reference's CPU implementation instead (its own
-generated kernel built for the host when available, else the CPU oracle in the
-reference's fp32 arithmetic) on all host threads, one bounded sample per step.
+`--impl reference` runs the reference arm: the reference algorithm on the host
+cores (its own generated kernel built for the host when available, else the
+CPU oracle in the reference's fp32 arithmetic) at its 1e-4 budget, one bounded
+sample per step.
 """
 from __future__ import annotations
 
@@ -46,16 +60,21 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 M_IVIM10 = 10
+M_IVIM16 = 16
 P_IVIM = 4
+TOL = 1e-4
+METRIC = "IVIM voxel fits/s at 1e-4 rel err vs FP64: MLP-warm-start vs plain LM, 1 GB300"
+# network FLOPs per voxel: 2 * (16*128 + 128*128 + 128*128 + 128*4)
+NET_FLOP_PER_VOXEL = 2 * (16 * 128 + 2 * 128 * 128 + 128 * 4)
 
 
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             pk = json.load(f)
-        return float(pk["hbm_gbs"]), "measured"
+        return float(pk["hbm_gbs"]), float(pk["bf16_tflops"]), "measured"
     except Exception:
-        return 6800.0, "fallback"
+        return 6800.0, 1900.0, "fallback"
 
 
 class ClockSampler:
@@ -121,53 +140,80 @@ def _dist():
     return ws, rank, local
 
 
-def cpu_sample(iters: int, target_s: float, dtype_mode: str = "reference", min_voxels: int = 16384,
-               parity_out: dict | None = None):
-    """Time the CPU reference implementation on a bounded IVIM-10 sample.
+# ---- CPU reference ------------------------------------------------------------
 
-    Uses the reference's generated kernel built for the host (oracle/_ref)
-    when present, else the CPU oracle in the reference's fp32 arithmetic. The
-    sample doubles until one run takes at least target_s/4 seconds, then the
-    last size is timed once. Returns (fits_per_s, kind, cores, sample_text).
-    With ``parity_out``, the GPU fitter is run on the same sample (FP64 solve
-    and fp32 solve) and its agreement with the CPU fit is recorded there.
+def _median_rel_np(a, b):
+    """Median over voxels of the worst per-parameter relative error, and the
+    fraction of voxels above 1e-4 (the GPU helper's definition)."""
+    r = np.abs(a.astype(np.float64) - b.astype(np.float64)) / np.maximum(np.abs(b.astype(np.float64)), 1e-30)
+    r = np.nan_to_num(r, nan=np.inf).max(axis=0)
+    return float(np.median(r)), float(np.mean(r > TOL))
+
+
+def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 30):
+    """The reference algorithm (plain LM, fp32) on the host cores, on IVIM-16
+    at the smallest iteration budget whose median error against the all-FP64
+    CPU fit (same LM, constant start, 300 iterations) is <= 1e-4. The sample
+    grows until one fit takes at least target_s / 4; that size is timed once.
     """
     from oracle import OracleModel, RefIVIM, ref_available
     from pycompute_gb300 import synth
 
-    w = synth.ivim()
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
     cores = os.cpu_count() or 1
-    if ref_available(M_IVIM10):
-        impl, kind = RefIVIM(M_IVIM10), "reference"
-        run = lambda p, d, i, lb, ub, prot: impl.lm_run(p, prot, d, lb, ub, iters)  # noqa: E731
+    port = OracleModel(w.expr, w.pars, w.consts)
+    port.set_threads(cores)
+    if ref_available(M_IVIM16):
+        impl, kind = RefIVIM(M_IVIM16), "reference"
     else:
-        impl, kind = OracleModel(w.expr, w.pars, w.consts), "port"
-        impl.set_threads(cores)
-        run = lambda p, d, i, lb, ub, prot: impl.lm_run(p, prot, d, lb, ub, iters)  # noqa: E731
-    n = min_voxels
+        impl, kind = port, "port"
+    _, data, init, lb, ub, prot = w.generate(n_ref, seed=7)
+    p64 = init.astype(np.float64)
+    port.lm_run(p64, prot.astype(np.float64), data.astype(np.float64), lb.astype(np.float64),
+                ub.astype(np.float64), 300, tol=1e-30)
+    curve, k_tol = {}, None
+    for k in range(1, max_iters + 1):
+        p = init.copy()
+        impl.lm_run(p, prot, data, lb, ub, k)
+        curve[k] = _median_rel_np(p, p64)[0]
+        if curve[k] <= TOL:
+            k_tol = k
+            break
+    k_run = k_tol if k_tol is not None else max_iters
+    n = 1 << 16
     while True:
-        true, data, init, lb, ub, prot = w.generate(n, seed=7)
+        _, data, init, lb, ub, prot = w.generate(n, seed=8)
         p = init.copy()
         t0 = time.perf_counter()
-        res = run(p, data, init, lb, ub, prot)
+        impl.lm_run(p, prot, data, lb, ub, k_run)
         el = time.perf_counter() - t0
-        if el >= target_s / 4 or n >= (1 << 22):
+        if el >= target_s / 4 or n >= (1 << 23):
             break
         n *= 2 if el > 0.05 else 8
-    sample = (f"{n} IVIM-10 voxels x {iters} iterations ({'reference generated kernel' if kind == 'reference' else 'fp32 oracle port'}, "
-              f"{cores} threads), {el:.2f} s")
-    if parity_out is not None:
-        parity_out.update(gpu_vs_cpu_parity(w, data, init, lb, ub, prot, p, res["step_type"], iters, kind))
-    return n / el, kind, cores, sample
+    what = "reference generated kernel" if kind == "reference" else "fp32 oracle port"
+    sample = (f"{n} IVIM-16 voxels x {k_run} iterations (the 1e-4 budget on {n_ref} voxels vs the all-FP64 CPU fit; "
+              f"{what}, {cores} threads), {el:.2f} s")
+    return {"value": n / el, "unit": "fits/s", "cores": cores, "kind": kind, "sample": sample, "iters": k_run,
+            "curve": curve}
 
 
-def gpu_vs_cpu_parity(w, data, init, lb, ub, prot, p_cpu, st_cpu, iters, kind):
-    """The GPU fitter on the CPU sample's inputs, compared with the CPU fit
-    (parameters and convergence flags, step_type == 0)."""
+def cpu_parity_ivim10(n: int = 1 << 18, iters: int = 100):
+    """The GPU fitter against the reference algorithm on the host, same IVIM-10
+    inputs: parameter agreement and convergence flags (step_type == 0)."""
     import torch
-    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, parity
+    from oracle import OracleModel, RefIVIM, ref_available
+    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, parity, synth
 
-    out = {"cpu": kind, "voxels": int(data.shape[1]), "iters": iters}
+    w = synth.ivim()
+    if ref_available(M_IVIM10):
+        impl, kind = RefIVIM(M_IVIM10), "reference"
+    else:
+        impl, kind = OracleModel(w.expr, w.pars, w.consts), "port"
+        impl.set_threads(os.cpu_count() or 1)
+    _, data, init, lb, ub, prot = w.generate(n, seed=7)
+    p_cpu = init.copy()
+    st_cpu = impl.lm_run(p_cpu, prot, data, lb, ub, iters)["step_type"]
+    out = {"cpu": kind, "voxels": n, "iters": iters}
     for solve, tdt in (("f64", torch.float64), ("f32", torch.float32)):
         solm = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float32,
                                              solve_dtype=tdt)
@@ -182,12 +228,19 @@ def gpu_vs_cpu_parity(w, data, init, lb, ub, prot, p_cpu, st_cpu, iters, kind):
     return out
 
 
+# ---- GPU helpers -------------------------------------------------------------
+
 def _median_rel_gpu(a, b):
     """Median over voxels of the worst per-parameter relative error (on the GPU)."""
     import torch
     r = (a.double() - b.double()).abs() / b.double().abs().clamp_min(1e-30)
     r = torch.nan_to_num(r, nan=float("inf")).amax(dim=0)
-    return float(r.median()), float((r > 1e-4).double().mean())
+    return float(r.median()), float((r > TOL).double().mean())
+
+
+def _per_param_median(a, b):
+    r = (a.double() - b.double()).abs() / b.double().abs().clamp_min(1e-30)
+    return [float(x) for x in r.median(dim=1).values]
 
 
 def _time_ms(fn, warmup=2, reps=3):
@@ -204,7 +257,7 @@ def _time_ms(fn, warmup=2, reps=3):
     return s.elapsed_time(e) / reps
 
 
-def budget_for_tolerance(run_with, ref, budgets, tol=1e-4):
+def budget_for_tolerance(run_with, ref, budgets, tol=TOL):
     """Smallest iteration budget whose fit has median relative error <= tol vs ref."""
     curve = {}
     for k in budgets:
@@ -229,74 +282,231 @@ def fp64_reference(w, data, iters=1000):
     return p
 
 
-def warm_start_comparison(n_eval=1 << 24, n_train=1 << 21, epochs=64, seed=77, lam0=3e-3):
-    """C5: IVIM-16, MLP warm start + LM + fallback vs plain LM, fits/s at 1e-4 vs FP64."""
+def _stage_ms(events, a, b):
+    """Elapsed ms between the events named a and b of one fit's event list."""
+    d = dict(events)
+    return d[a].elapsed_time(d[b])
+
+
+# ---- headline: warm start vs plain LM at 1e-4 -----------------------------------
+
+def warm_headline(args, ws, rank, local, dev):
+    """IVIM-16: network + LM + fallback vs plain LM, both at their 1e-4 budgets."""
     import torch
+    import torch.distributed as dist
     from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline, synth
+    from pycompute_gb300.shard import max_over_ranks
     from pycompute_gb300.warmstart import WarmStartMLP
-    dev = torch.device("cuda")
+
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     expr = Expr(w.expr, w.pars, w.consts)
-    prot = torch.tensor(w.protocol, device=dev)
-    lb = torch.tensor(w.lb, device=dev)
-    ub = torch.tensor(w.ub, device=dev)
+    N = args.warm_voxels
     t0 = time.perf_counter()
-    _, tr = pipeline.synth_gpu(w, n_train, seed=seed, device=dev)
+    # training set: other synthetic signals, labels = the plain LM's converged fits
+    _, tr = pipeline.synth_gpu(w, args.warm_train, seed=77 + 1000 * rank, device=dev)
     lab = pipeline.init_constant(tr, w.init_values)
     s = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32)
-    s.setup(lab, prot, tr, lb, ub)
+    s.setup(lab, list(w.protocol), tr, list(w.lb), list(w.ub))
     s.run(100)
-    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, dev, seed=seed)
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, dev, seed=77)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    net.train(tr, lab, epochs=epochs, batch=8192, lr=2e-3)
+    net.train(tr, lab, epochs=args.warm_epochs, batch=8192, lr=2e-3)
+    torch.cuda.synchronize()
     train_s = time.perf_counter() - t1
     del tr, lab, s
-    _, data = pipeline.synth_gpu(w, n_eval, seed=seed + 1, device=dev)
+    # evaluation voxels (each rank its own shard) and their FP64 reference
+    _, data = pipeline.synth_gpu(w, N, seed=78 + 1000 * rank, device=dev)
     ref = fp64_reference(w, data, iters=300)
-    pars = torch.empty((4, n_eval), device=dev)
+    pars = torch.empty((4, N), device=dev)
     plain = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32)
 
     def run_plain(k):
         pipeline.init_constant(data, w.init_values, out=pars)
-        plain.setup(pars, prot, data, lb, ub)
+        plain.setup(pars, list(w.protocol), data, list(w.lb), list(w.ub))
         plain.run(k)
         return pars
 
     wf = pipeline.WarmStartFitter(w, net)
-    state = {}
-
-    def run_warm(k, timings=None):
-        state["res"] = wf.fit(data, iters_warm=k, iters_fallback=k_plain or 30, pars_out=pars, lam0=lam0,
-                              timings=timings)
-        return state["res"]["pars"]
-
+    lam0 = args.warm_lam0
     k_plain, curve_plain = budget_for_tolerance(run_plain, ref, range(1, 31))
-    k_warm, curve_warm = budget_for_tolerance(run_warm, ref, range(0, 21))
-    out = {"workload": "ivim16_warm_vs_plain", "voxels": n_eval, "train_voxels": n_train, "epochs": epochs,
-           "train_s": round(train_s, 3), "setup_s": round(time.perf_counter() - t0, 1),
-           "plain_iters_for_1e-4": k_plain, "warm_iters_for_1e-4": k_warm,
-           "plain_curve": {k: v[0] for k, v in curve_plain.items()},
-           "warm_curve": {k: v[0] for k, v in curve_warm.items()}}
-    if k_plain is not None:
-        ms = _time_ms(lambda: run_plain(k_plain))
-        med, frac = _median_rel_gpu(run_plain(k_plain), ref)
-        out["plain"] = {"fits_per_s": n_eval / (ms / 1e3), "ms": ms, "median_rel_err": med, "frac_gt_1e-4": frac}
-    if k_warm is not None:
-        ms = _time_ms(lambda: run_warm(k_warm))
-        med, frac = _median_rel_gpu(run_warm(k_warm), ref)
-        tm = {}
-        run_warm(k_warm, timings=tm)
-        out["warm"] = {"fits_per_s": n_eval / (ms / 1e3), "ms": ms, "median_rel_err": med, "frac_gt_1e-4": frac,
-                       "fallback_voxels": state["res"]["n_fallback"], "refits_kept": state["res"]["n_refit_kept"],
-                       "stage_ms": {k: round(v, 3) for k, v in tm.items()}}
-    if "plain" in out and "warm" in out:
-        out["speedup"] = out["warm"]["fits_per_s"] / out["plain"]["fits_per_s"]
+    k_fb = k_plain or 30
+
+    def run_warm(k, data_in=data, out=pars, events=None):
+        return wf.fit(data_in, iters_warm=k, iters_fallback=k_fb, pars_out=out, lam0=lam0, events=events)
+
+    k_warm, curve_warm = budget_for_tolerance(lambda k: run_warm(k).pars, ref, range(0, 21))
+    setup_s = time.perf_counter() - t0
+    if k_warm is None or k_plain is None:
+        raise RuntimeError(f"no budget reached {TOL}: plain {curve_plain}, warm {curve_warm}")
+
+    # ---- timed: warm-start steps, device resident --------------------------
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        run_warm(k_warm)
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    step_events = []
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        t_start.record(stream)
+        for _ in range(args.steps):
+            ev = []
+            res = run_warm(k_warm, events=ev)
+            step_events.append(ev)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    step_ms = t_start.elapsed_time(t_end) / args.steps
+    stages = {}
+    for a, b in (("start", "network"), ("network", "setup"), ("setup", "lm_warm"), ("lm_warm", "check"),
+                 ("check", "refit"), ("refit", "select")):
+        stages[b] = statistics.mean(_stage_ms(ev, a, b) for ev in step_events)
+    step_ms, lm_ms, net_ms = max_over_ranks([step_ms, stages["lm_warm"], stages["network"]], device=dev)
+    med_w, frac_w = _median_rel_gpu(res.pars, ref)
+    pp_w = _per_param_median(res.pars, ref)
+    warm_pars_h = res.pars.cpu()
+    n_fb, n_kept = res.n_fallback, res.n_refit_kept
+
+    # ---- plain LM at its budget, same voxels --------------------------------
+    plain_ms = _time_ms(lambda: run_plain(k_plain), warmup=max(1, args.warmup), reps=args.steps)
+    plain_ms = max_over_ranks([plain_ms], device=dev)[0]
+    p_plain = run_plain(k_plain)
+    med_p, frac_p = _median_rel_gpu(p_plain, ref)
+    pp_p = _per_param_median(p_plain, ref)
+
+    # ---- end to end through the public API from pinned host buffers ---------
+    data_h = data.cpu().pin_memory()
+    out_h = torch.empty((4, N), dtype=torch.float32).pin_memory()
+    data_e = torch.empty_like(data)
+    pars_e = torch.empty((4, N), device=dev)
+
+    def e2e_step():
+        data_e.copy_(data_h, non_blocking=True)
+        run_warm(k_warm, data_in=data_e, out=pars_e)
+        out_h.copy_(pars_e, non_blocking=True)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e_start.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e_end.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks([e_start.elapsed_time(e_end) / args.steps], device=dev)[0]
+    e2e_same = bool(torch.equal(out_h, warm_pars_h))
+
+    return {
+        "N": N, "step_ms": step_ms, "plain_ms": plain_ms, "e2e_ms": e2e_ms, "lm_ms": lm_ms, "net_ms": net_ms,
+        "stages": stages, "clocks": clk.summary(), "h2d": data_h.nbytes, "d2h": out_h.nbytes,
+        "k_warm": k_warm, "k_plain": k_plain, "e2e_same": e2e_same,
+        "detail": {
+            "train_voxels": args.warm_train, "epochs": args.warm_epochs, "train_s": round(train_s, 3),
+            "setup_s": round(setup_s, 1), "lam0": lam0,
+            "warm_curve": {k: v[0] for k, v in curve_warm.items()},
+            "plain_curve": {k: v[0] for k, v in curve_plain.items()},
+            "warm_accuracy": {"median_rel_err": med_w, "frac_voxels_gt_1e-4": frac_w, "per_param_median": pp_w},
+            "plain_accuracy": {"median_rel_err": med_p, "frac_voxels_gt_1e-4": frac_p, "per_param_median": pp_p},
+            "fallback_voxels": n_fb, "refits_kept": n_kept,
+            "stage_ms": {k: round(v, 3) for k, v in stages.items()},
+            "accuracy_reference": "all-FP64 GPU fit, same LM, constant start, 300 iterations, tol 1e-30",
+        },
+    }
+
+
+# ---- secondary: plain LM at scale, IVIM-10 ------------------------------------------
+
+def plain_ivim10_block(args, dev, fp64_check=True):
+    """IVIM-10, 8,388,608 voxels, plain LM, 100 iterations (the reference's
+    run(100) at scale): fits/s, kernel time, accuracy against the FP64 fitter
+    and fits/s at the 1e-4 budget."""
+    import torch
+    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, parity, synth
+
+    w = synth.ivim()
+    N = args.voxels
+    true, data, init, lb, ub, prot = w.generate(N, seed=1000)
+    solve = torch.float64 if args.solve == "f64" else torch.float32
+    expr = Expr(w.expr, w.pars, w.consts)
+    solm = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32, solve_dtype=solve)
+    data_d = torch.from_numpy(data).to(dev)
+    init_d = torch.from_numpy(init).to(dev)
+    pars_d = init_d.clone()
+    solm.setup(pars_d, [float(x) for x in prot], data_d, [float(x) for x in lb], [float(x) for x in ub])
+
+    def reset():
+        pars_d.copy_(init_d)
+        solm.lam_t.fill_(5.0)
+        solm.step_type_t.fill_(1)
+        solm.f_t.zero_()
+        solm.iters_t.zero_()
+
+    for _ in range(args.warmup):
+        reset()
+        solm.run(args.iters, block=args.block)
+    torch.cuda.synchronize()
+    ks = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ke = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0.record()
+    for s in range(args.steps):
+        reset()
+        ks[s].record()
+        solm.run(args.iters, block=args.block)
+        ke[s].record()
+    t1.record()
+    torch.cuda.synchronize()
+    step_ms = t0.elapsed_time(t1) / args.steps
+    kern_ms = statistics.mean(ks[s].elapsed_time(ke[s]) for s in range(args.steps))
+    fitted = pars_d.cpu().numpy()
+    its = solm.iters_t.cpu().numpy()[0].astype(np.int64)
+    st = solm.step_type_t.cpu().numpy()[0]
+    hbm, _, peak_kind = _peaks()
+    bpv = 4 * M_IVIM10 + 4 * P_IVIM + 1
+    out = {"workload": "ivim10_plain_lm_8.4M", "voxels": N, "iters": args.iters, "solve": args.solve,
+           "fits_per_s": N / (step_ms / 1e3), "ms_per_step": step_ms, "kernel_ms": kern_ms,
+           "mean_iters": float(its.mean()), "converged_frac": float(np.mean(st == 0)),
+           "voxel_iters_per_s": float(its.sum()) / (kern_ms / 1e3),
+           "hbm_roofline": {"achieved_gbs": bpv * N / (kern_ms / 1e3) / 1e9, "peak_gbs": hbm,
+                            "algorithmic_bytes_per_voxel": bpv, "peak_source": peak_kind}}
+    if fp64_check:
+        dd = data_d.double()
+        solm64 = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float64)
+        p64 = init_d.double()
+        solm64.setup(p64, torch.from_numpy(prot).to(dev).double(), dd, torch.from_numpy(lb).to(dev).double(),
+                     torch.from_numpy(ub).to(dev).double())
+        solm64.run(args.iters)
+        torch.cuda.synchronize()
+        rep = parity.compare_params(fitted, p64.cpu().numpy())
+        out["accuracy"] = {"vs": "all-FP64 GPU fitter, same LM, init and iterations",
+                           "median_rel_err": rep["median_rel"], "frac_voxels_gt_1e-4": rep["frac_gt_1e-4"],
+                           "per_param_median": rep["per_param_median"],
+                           "converged_frac_fp64": float(np.mean(solm64.step_type_t.cpu().numpy() == 0))}
+        del solm64, p64, dd
+        ref64 = fp64_reference(w, data_d, iters=1000)
+
+        def run_k(k):
+            reset()
+            solm.run(k, block=args.block)
+            return pars_d
+
+        k_tol, curve = budget_for_tolerance(run_k, ref64, range(2, 41))
+        at = {"iters": k_tol, "curve": {k: v[0] for k, v in curve.items()}}
+        if k_tol is not None:
+            at["fits_per_s"] = N / (_time_ms(lambda: run_k(k_tol)) / 1e3)
+        out["at_1e-4_vs_fp64"] = at
     return out
 
 
 def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
-    """C3: VFA-T1 + T2* + IVIM + bi-exp T2, 1M voxels each, one persistent
+    """VFA-T1 + T2* + IVIM + bi-exp T2, 1M voxels each, one persistent
     launch (autotuned) vs one single-model launch per model."""
     import torch
     from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline, synth
@@ -365,22 +575,31 @@ def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
             "ms": {"one_launch": ms_multi, "graph": ms_graph, "per_model": ms_single}}
 
 
+def _config(args, ws, k_warm=None, k_plain=None):
+    return {"workload": "ivim16_warm_start_vs_plain_lm_16.7M", "voxels_per_gpu": args.warm_voxels,
+            "ndata": M_IVIM16, "nparam": P_IVIM, "tolerance": TOL, "iters_warm": k_warm, "iters_plain": k_plain,
+            "network": "16-128-128-128-4 GELU, bf16 weights, fp32 accumulate",
+            "train_voxels": args.warm_train, "solve": "f64", "init_plain": "constant [max S, 0.1, 1e-2, 1e-3]",
+            "l2": "inputs larger than L2 (1.07 GB signals per GPU)", "parallelism": f"voxel shards x{ws}"}
+
+
 def run_reference_arm(args):
     ws, rank, local = _dist()
     if rank != 0:
         return 0
-    vals = []
+    vals, last = [], None
     for s in range(args.warmup + args.steps):
-        v, kind, cores, sample = cpu_sample(args.iters, target_s=args.cpu_seconds, min_voxels=16384)
+        last = cpu_reference_at_tol(target_s=args.cpu_seconds)
         if s >= args.warmup:
-            vals.append(v)
+            vals.append(last["value"])
     value = statistics.median(vals)
     line = {
-        "impl": "reference", "metric": "IVIM voxel fits/s", "value": value, "unit": "fits/s", "n_gpus": args.gpus,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded IVIM-10, Rician SNR 50)",
-        "config": {"workload": "ivim10_plain_lm_cpu_sample", "iters": args.iters},
-        "cpu_baseline": {"value": value, "unit": "fits/s", "cores": cores, "kind": kind, "sample": sample},
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded IVIM-16, Rician SNR 50)",
+        "config": dict(_config(args, 1, None, last["iters"]), method="plain LM (the reference has no warm start)"),
+        "cpu_baseline": {"value": value, "unit": "fits/s", "cores": last["cores"], "kind": last["kind"],
+                         "sample": last["sample"]},
         "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -393,219 +612,96 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--voxels", type=int, default=256 * 256 * 128)
-    ap.add_argument("--iters", type=int, default=100)
-    ap.add_argument("--solve", default="f64", choices=["f64", "f32"])
-    ap.add_argument("--block", type=int, default=0)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-fp64-check", action="store_true")
-    ap.add_argument("--no-warm", action="store_true", help="skip the warm-start comparison (IVIM-16)")
     ap.add_argument("--warm-voxels", type=int, default=1 << 24)
-    ap.add_argument("--only-warm", action="store_true", help="run only the warm-start comparison")
-    ap.add_argument("--only-mixed", action="store_true", help="run only the mixed-model batch comparison")
-    ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--warm-epochs", type=int, default=64)
     ap.add_argument("--warm-lam0", type=float, default=3e-3)
     ap.add_argument("--warm-train", type=int, default=1 << 21)
+    ap.add_argument("--voxels", type=int, default=256 * 256 * 128, help="IVIM-10 plain-LM block")
+    ap.add_argument("--iters", type=int, default=100, help="IVIM-10 plain-LM block")
+    ap.add_argument("--solve", default="f64", choices=["f64", "f32"], help="IVIM-10 plain-LM block")
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ivim10", action="store_true", help="skip the IVIM-10 plain-LM block")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-fp64-check", action="store_true", help="IVIM-10 block without its FP64 comparison")
+    ap.add_argument("--only-ivim10", action="store_true", help="print only the IVIM-10 plain-LM block")
+    ap.add_argument("--only-mixed", action="store_true", help="print only the mixed-model block")
+    ap.add_argument("--only-warm", action="store_true", help="print only the warm-start headline fields")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference_arm(args)
-    if args.only_mixed:
-        print(json.dumps(mixed_batch_comparison()), flush=True)
-        return 0
-    if args.only_warm:
-        print(json.dumps(warm_start_comparison(n_eval=args.warm_voxels, epochs=args.warm_epochs,
-                                               lam0=args.warm_lam0, n_train=args.warm_train)), flush=True)
-        return 0
 
     import torch
     import torch.distributed as dist
 
-    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, parity, synth
-
-    from pycompute_gb300.shard import max_over_ranks
-
     ws, rank, local = _dist()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.only_mixed:
+        print(json.dumps(mixed_batch_comparison()), flush=True)
+        return 0
+    if args.only_ivim10:
+        print(json.dumps(plain_ivim10_block(args, dev, fp64_check=not args.no_fp64_check)), flush=True)
+        return 0
     if ws > 1:
         dist.init_process_group("nccl", device_id=dev)
 
-    w = synth.ivim()
-    N = args.voxels
-    # each rank fits its own shard (weak scaling): seeds differ per rank
-    true, data, init, lb, ub, prot = w.generate(N, seed=1000 + rank)
-    solve = torch.float64 if args.solve == "f64" else torch.float32
-    expr = Expr(w.expr, w.pars, w.consts)
-    solm = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32, solve_dtype=solve)
-
-    data_d = torch.from_numpy(data).to(dev)
-    init_d = torch.from_numpy(init).to(dev)
-    prot_d = torch.from_numpy(prot).to(dev)
-    lb_d = torch.from_numpy(lb).to(dev)
-    ub_d = torch.from_numpy(ub).to(dev)
-    pars_d = init_d.clone()
-    solm.setup(pars_d, prot_d, data_d, lb_d, ub_d)
-    stream = torch.cuda.current_stream()
-
-    def reset():
-        pars_d.copy_(init_d)
-        solm.lam_t.fill_(5.0)
-        solm.step_type_t.fill_(1)
-        solm.f_t.zero_()
-        solm.iters_t.zero_()
-
-    # ---- device-resident timing -------------------------------------------
-    for _ in range(args.warmup):
-        reset()
-        solm.run(args.iters, block=args.block)
-    torch.cuda.synchronize()
-    k_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    k_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    t_start = torch.cuda.Event(enable_timing=True)
-    t_end = torch.cuda.Event(enable_timing=True)
-    if ws > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
-        t_start.record(stream)
-        for s in range(args.steps):
-            reset()
-            k_start[s].record(stream)
-            solm.run(args.iters, block=args.block)
-            k_end[s].record(stream)
-        t_end.record(stream)
-        torch.cuda.synchronize()
-    if ws > 1:
-        dist.barrier()
-    step_ms = t_start.elapsed_time(t_end) / args.steps
-    kern_ms = statistics.mean(k_start[s].elapsed_time(k_end[s]) for s in range(args.steps))
-    step_ms, kern_ms = max_over_ranks([step_ms, kern_ms], device=dev)
-    fitted = pars_d.cpu().numpy()
-    st = solm.step_type_t.cpu().numpy()[0]
-    its = solm.iters_t.cpu().numpy()[0].astype(np.int64)
-
-    # ---- end to end through the public API from pinned host buffers -------
-    data_h = torch.from_numpy(data).pin_memory()
-    init_h = torch.from_numpy(init).pin_memory()
-    out_pars_h = torch.empty_like(init_h).pin_memory()
-    out_st_h = torch.empty((1, N), dtype=torch.int8).pin_memory()
-    data_e = torch.empty_like(data_d)
-    pars_e = torch.empty_like(init_d)
-    solm_e = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32, solve_dtype=solve)
-
-    def e2e_step():
-        data_e.copy_(data_h, non_blocking=True)
-        pars_e.copy_(init_h, non_blocking=True)
-        solm_e.setup(pars_e, prot_d, data_e, lb_d, ub_d)
-        solm_e.run(args.iters, block=args.block)
-        out_pars_h.copy_(pars_e, non_blocking=True)
-        out_st_h.copy_(solm_e.step_type_t, non_blocking=True)
-
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    torch.cuda.synchronize()
-    if ws > 1:
-        dist.barrier()
-    e_start = torch.cuda.Event(enable_timing=True)
-    e_end = torch.cuda.Event(enable_timing=True)
-    e_start.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    e_end.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = max_over_ranks([e_start.elapsed_time(e_end) / args.steps], device=dev)[0]
-    assert np.array_equal(out_pars_h.numpy(), fitted), "e2e result differs from the device-resident run"
-    h2d = data.nbytes + init.nbytes
-    d2h = init.nbytes + N
-
-    # ---- accuracy against the all-FP64 fitter (untimed) -------------------
-    acc = None
-    if not args.no_fp64_check:
-        solm64 = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float64)
-        p64 = init_d.double()
-        solm64.setup(p64, prot_d.double(), data_d.double(), lb_d.double(), ub_d.double())
-        t0 = time.perf_counter()
-        solm64.run(args.iters)
-        torch.cuda.synchronize()
-        t64 = time.perf_counter() - t0
-        rep = parity.compare_params(fitted, p64.cpu().numpy())
-        acc = {"vs": "all-FP64 GPU fitter, same LM and init", "median_rel_err": rep["median_rel"],
-               "frac_voxels_gt_1e-4": rep["frac_gt_1e-4"], "per_param_median": rep["per_param_median"],
-               "converged_frac_fp64": float(np.mean(solm64.step_type_t.cpu().numpy() == 0)),
-               "fp64_fit_s": round(t64, 3)}
-        del p64, solm64
-
-    # ---- fits/s at the budget that reaches 1e-4 median error vs FP64 -------
-    at_tol = None
-    if not args.no_fp64_check:
-        ref64 = fp64_reference(w, data_d)
-
-        def run_k(k):
-            reset()
-            solm.run(k, block=args.block)
-            return pars_d
-
-        k_tol, curve = budget_for_tolerance(run_k, ref64, range(2, 41))
-        at_tol = {"iters": k_tol, "curve": {k: v[0] for k, v in curve.items()}}
-        if k_tol is not None:
-            ms = _time_ms(lambda: run_k(k_tol))
-            at_tol["fits_per_s"] = ws * N / (ms / 1e3)
-        del ref64
-
-    warm = None
-    if rank == 0 and ws == 1 and not args.no_warm:
-        warm = warm_start_comparison(n_eval=args.warm_voxels, epochs=args.warm_epochs, lam0=args.warm_lam0,
-                                     n_train=args.warm_train)
-
-    mixed = None
-    if rank == 0 and ws == 1 and not args.no_mixed:
-        mixed = mixed_batch_comparison()
-
-    # ---- CPU baseline (rank 0, N=1 only) ----------------------------------
+    h = warm_headline(args, ws, rank, local, dev)
+    if args.only_warm:
+        if rank == 0:
+            print(json.dumps({k: v for k, v in h.items() if k != "clocks"}), flush=True)
+        if ws > 1:
+            dist.destroy_process_group()
+        return 0
+    N = h["N"]
+    single = rank == 0 and ws == 1
+    ivim10 = plain_ivim10_block(args, dev, fp64_check=not args.no_fp64_check) if single and not args.no_ivim10 \
+        else None
+    mixed = mixed_batch_comparison() if single and not args.no_mixed else None
     cpu = None
-    if rank == 0 and ws == 1 and not args.no_cpu:
-        par = {}
-        v, kind, cores, sample = cpu_sample(args.iters, target_s=args.cpu_seconds, parity_out=par)
-        cpu = {"value": v, "unit": "fits/s", "cores": cores, "kind": kind, "sample": sample, "gpu_parity": par}
+    if single and not args.no_cpu:
+        cpu = cpu_reference_at_tol(target_s=args.cpu_seconds)
+        cpu["gpu_parity_ivim10"] = cpu_parity_ivim10()
 
     if rank == 0:
-        hbm, peak_kind = _peaks()
-        bytes_per_voxel = 4 * M_IVIM10 + 4 * P_IVIM + 1
-        achieved = bytes_per_voxel * N / (kern_ms / 1e3) / 1e9
+        hbm, bf16_peak, peak_kind = _peaks()
+        bpv = 4 * M_IVIM16 + 8 * P_IVIM + 1
+        lm_gbs = bpv * N / (h["lm_ms"] / 1e3) / 1e9
+        net_tf = NET_FLOP_PER_VOXEL * N / (h["net_ms"] / 1e3) / 1e12
         traffic = None
-        tf = os.path.join(ROOT, "profiles", "lm_ivim10_traffic.json")
+        tf = os.path.join(ROOT, "profiles", "lm_ivim16_warm_traffic.json")
         if os.path.exists(tf):
             with open(tf) as f:
-                tr = json.load(f)
-            traffic = tr["dram_bytes_per_voxel"] * N
-        value = ws * N / (step_ms / 1e3)
+                traffic = json.load(f)["dram_bytes_per_voxel"] * N
+        value = ws * N / (h["step_ms"] / 1e3)
+        plain_value = ws * N / (h["plain_ms"] / 1e3)
         line = {
-            "metric": "IVIM voxel fits/s (plain LM, 100 iters max)", "value": value, "unit": "fits/s",
-            "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 (f64 GMW81 solve + gain ratio)" if args.solve == "f64" else "f32",
-            "data": "synthetic (seeded IVIM-10, Rician SNR 50)",
-            "config": {"workload": "ivim10_plain_lm_8.4M", "voxels_per_gpu": N, "ndata": M_IVIM10,
-                       "nparam": P_IVIM, "iters": args.iters, "solve": args.solve, "init": "constant",
-                       "l2": "inputs larger than L2 (335 MB signals)", "parallelism": f"voxel shards x{ws}"},
-            "e2e": {"value": ws * N / (e2e_ms / 1e3), "unit": "fits/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": traffic, "peak_source": peak_kind,
-                         "algorithmic_bytes_per_voxel": bytes_per_voxel,
-                         "note": "iterative per-voxel solver: FP64/FP32 issue bound, not HBM bound"},
-            "kernel_ms": kern_ms,
-            "fit_stats": {"mean_iters": float(its.mean()), "converged_frac": float(np.mean(st == 0)),
-                          "voxel_iters_per_s": float(its.sum()) * ws / (kern_ms / 1e3)},
-            "accuracy": acc,
-            "at_1e-4_vs_fp64": at_tol,
-            "warm_start": warm,
+            "metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": h["step_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 state, f64 GMW81 solve + gain ratio, bf16 network",
+            "data": "synthetic (seeded IVIM-16, Rician SNR 50; network trained on other seeded signals)",
+            "config": _config(args, ws, h["k_warm"], h["k_plain"]),
+            "plain_lm": {"value": plain_value, "unit": "fits/s", "ms_per_step": h["plain_ms"],
+                         "iters": h["k_plain"], "speedup_warm_vs_plain": value / plain_value},
+            "e2e": {"value": ws * N / (h["e2e_ms"] / 1e3), "unit": "fits/s", "h2d_bytes_per_step": h["h2d"],
+                    "d2h_bytes_per_step": h["d2h"], "ms_per_step": h["e2e_ms"],
+                    "matches_device_run": h["e2e_same"]},
+            "roofline": {"bound": "hbm", "achieved": lm_gbs, "peak": hbm, "unit": "GB/s", "frac": lm_gbs / hbm,
+                         "traffic": traffic, "peak_source": peak_kind, "kernel": "pcgb_lm (warm LM stage)",
+                         "algorithmic_bytes_per_voxel": bpv, "kernel_ms": h["lm_ms"],
+                         "note": "per-voxel iterative solver: bound by the FP64 pipe (GMW81 solve + gain ratio), "
+                                 "not by HBM; ncu summaries in profiles/"},
+            "roofline_network": {"bound": "tensor", "achieved": net_tf, "peak": bf16_peak, "unit": "TFLOP/s",
+                                 "frac": net_tf / bf16_peak, "kernel": "mlp_infer_tc_kernel (tcgen05)",
+                                 "flop_per_voxel": NET_FLOP_PER_VOXEL, "kernel_ms": h["net_ms"],
+                                 "peak_source": peak_kind},
+            "warm_start": h["detail"],
+            "plain_lm_ivim10_8.4M": ivim10,
             "mixed_batch": mixed,
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps,
-            "clocks": clk.summary(),
+            "gpu_launches": 5 * args.steps,
+            "clocks": h["clocks"],
         }
         print(json.dumps(line), flush=True)
     if ws > 1:

@@ -115,14 +115,17 @@ int pcgb_lm_run(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, 
  * pcgb_lm_run restricted to the n_items voxels listed in vox_idx (int32
  * device array of distinct voxel indices < nprobs); all other voxels are left
  * untouched. Used to refit a compacted subset (the warm-start fallback) in
- * one launch without gathering its data. No reference counterpart.
+ * one launch without gathering its data. n_items_dev (may be NULL): a device
+ * word with the list's length; then the first min(*n_items_dev, n_items)
+ * entries are fitted and the launch covers n_items. No reference counterpart.
  */
 int pcgb_lm_run_subset(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
                        const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
                        double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
                        void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
                        const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
-                       int block, const int32_t* vox_idx, int64_t n_items, void* stream);
+                       int block, const int32_t* vox_idx, int64_t n_items, const uint32_t* n_items_dev,
+                       void* stream);
 
 /*
  * pcgb_lm_run with the refill schedule: a persistent grid in which every lane
@@ -321,11 +324,13 @@ const char* pcgb_noalloc_last_error(void);
 /* Last error of the pipeline entry points on this host thread. */
 const char* pcgb_pipeline_last_error(void);
 
-/* y[i] = 1/x[i] by the FP64 reciprocal of the FP64 GMW81 solve (float seed and
- * two Newton-Raphson steps; zero, Inf, NaN and exponents outside the float
- * range take the correctly rounded reciprocal). Within 1 ulp of 1/x; exposed
- * so callers and tests can check that bound on their own inputs. */
-int pcgb_rcp64(const double* x, double* y, int64_t n, void* stream);
+/* The integer-pipe helpers of the FP64 GMW81 solve, elementwise, exposed so
+ * callers and tests can check them on their own inputs: rcp[i] = 1/x[i] by a
+ * float seed and one third-order Newton-Raphson step (within 1 ulp of 1/x;
+ * zero, Inf, NaN and exponents outside the float range take the correctly
+ * rounded reciprocal); narrowed[i] = x[i] rounded to float (to nearest even,
+ * equal to the hardware conversion). Either output may be NULL. */
+int pcgb_fp64_helpers(const double* x, double* rcp, float* narrowed, int64_t n, void* stream);
 
 /* Constant initialisation: pars[k][v] = values[k]; a NaN entry means "the
  * voxel's largest sample" (the reference notebooks' S0 start). */

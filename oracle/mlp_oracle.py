@@ -22,13 +22,24 @@ def bf16(x) -> np.ndarray:
 _C = np.sqrt(2.0 / np.pi)
 
 
+def _tanh_arg(z):
+    """u = z (c + c' z^2) rounded as the GPU evaluates it: z, z^2, the fused
+    c' z^2 + c and the product each rounded to float16 (overflow -> +-Inf)."""
+    with np.errstate(over="ignore", invalid="ignore"):
+        h = lambda v: np.asarray(v, dtype=np.float64).astype(np.float16).astype(np.float64)  # noqa: E731
+        zh = h(np.asarray(z, dtype=np.float32))
+        q = h(h(zh * zh) * float(np.float16(0.044715 * _C)) + float(np.float16(_C)))
+        return h(zh * q)
+
+
 def gelu(z):
-    """GELU, tanh form (Hendrycks & Gimpel 2016), as the GPU kernels use it."""
-    return 0.5 * z * (1.0 + np.tanh(_C * (z + 0.044715 * z ** 3)))
+    """GELU, tanh form (Hendrycks & Gimpel 2016), with the tanh argument rounded
+    to float16 as the GPU kernels compute it (tanh itself exact here)."""
+    return 0.5 * z * (1.0 + np.tanh(_tanh_arg(z)))
 
 
 def gelu_grad(z):
-    t = np.tanh(_C * (z + 0.044715 * z ** 3))
+    t = np.tanh(_tanh_arg(z))
     return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C * (1.0 + 3 * 0.044715 * z * z)
 
 

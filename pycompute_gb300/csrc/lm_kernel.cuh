@@ -55,8 +55,29 @@ PCGB_HD double pcgb_pow(double x, double y) { return pow(x, y); }
 namespace pcgb {
 
 template <typename T> struct Num;
+// sqrt(P^2 - 1), correctly rounded in each precision, for P = 2..8: the GMW81
+// scale of the largest off-diagonal entry (solver.py:32-57) as a literal, so
+// no square root or division of a constant runs per solve
+PCGB_HD constexpr float sqrt_pm1_f(int P) {
+  return P == 2 ? 1.7320507764816284f : P == 3 ? 2.8284270763397217f : P == 4 ? 3.872983455657959f
+       : P == 5 ? 4.898979663848877f : P == 6 ? 5.916079998016357f : P == 7 ? 6.928203105926514f
+       : 7.937253952026367f;
+}
+PCGB_HD constexpr double sqrt_pm1_d(int P) {
+  return P == 2 ? 1.7320508075688772 : P == 3 ? 2.8284271247461903 : P == 4 ? 3.872983346207417
+       : P == 5 ? 4.898979485566356 : P == 6 ? 5.916079783099616 : P == 7 ? 6.928203230275509
+       : 7.937253933193772;
+}
+// 1 / sqrt(P^2 - 1) rounded to double
+PCGB_HD constexpr double inv_sqrt_pm1_d(int P) {
+  return P == 2 ? 0.5773502691896258 : P == 3 ? 0.35355339059327373 : P == 4 ? 0.2581988897471611
+       : P == 5 ? 0.20412414523193154 : P == 6 ? 0.1690308509457033 : P == 7 ? 0.14433756729740646
+       : 0.1259881576697424;
+}
+
 template <> struct Num<float> {
   static PCGB_HD float gmw_eps() { return 2e-7f; }    // solver.py:105
+  static PCGB_HD constexpr float sqrt_pm1(int P) { return sqrt_pm1_f(P); }
   static PCGB_HD float damp_floor() { return 1e-4f; } // lsqnonlin.py:275
   static PCGB_HD float prot(const PcgbLmParams& a, int i) { return a.protocol_f[i]; }
   static PCGB_HD float slb(const PcgbLmParams& a, int k) { return a.shared_lb_f[k]; }
@@ -65,6 +86,7 @@ template <> struct Num<float> {
 };
 template <> struct Num<double> {
   static PCGB_HD double gmw_eps() { return 4e-16; }   // solver.py:109
+  static PCGB_HD constexpr double sqrt_pm1(int P) { return sqrt_pm1_d(P); }
   static PCGB_HD double damp_floor() { return 1e-4; } // lsqnonlin.py:278
   static PCGB_HD double prot(const PcgbLmParams& a, int i) { return a.protocol_d[i]; }
   static PCGB_HD double slb(const PcgbLmParams& a, int k) { return a.shared_lb_d[k]; }
@@ -121,7 +143,7 @@ PCGB_HD void gmw81_solve(const T (&A)[P * (P + 1) / 2], const T (&b)[P], T (&x)[
         if (t > nu) nu = t;
       }
     }
-  if (P > 1) nu /= pcgb_sqrt(T(P * P - 1));
+  if (P > 1) nu /= Num<T>::sqrt_pm1(P);
   if (beta2 < gam) beta2 = gam;
   if (beta2 < nu) beta2 = nu;
   if (gam + nu > T(1)) delta *= (gam + nu);
@@ -194,8 +216,16 @@ PCGB_HD void gmw81_solve(const T (&A)[P * (P + 1) / 2], const T (&b)[P], T (&x)[
 // few FP64 ulps (and by fp32 rounding in the scale factors, which precondition
 // the system and cancel out of the solution up to that rounding).
 
+// The two 32-bit words of a double, through an opaque move: the compiler
+// would otherwise recognise a masked sign bit as fabs and emit it as an FP64
+// add with an absolute-value operand (a DADD per use, on the FP64 pipe).
+PCGB_HD void words(double x, unsigned& lo, unsigned& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+}
 PCGB_HD unsigned long long abs_bits(double x) {
-  return static_cast<unsigned long long>(__double_as_longlong(x)) & 0x7fffffffffffffffULL;
+  unsigned lo, hi;
+  words(x, lo, hi);
+  return (static_cast<unsigned long long>(hi & 0x7fffffffu) << 32) | lo;
 }
 // m = max(m, |x|) on bit patterns, NaN skipped (bit patterns above +Inf).
 PCGB_HD void max_abs_bits(unsigned long long& m, double x) {
@@ -219,10 +249,31 @@ PCGB_HD double widen(float x) {
   return static_cast<double>(x);
 }
 
-// 1/x in FP64 by Newton-Raphson iteration (Markstein, IBM J. Res. Dev. 34,
-// 1990): a float seed from the float reciprocal of x's truncated high word
-// (relative error < 2^-19), then two steps y <- y + y (1 - x y), each squaring
-// the error (< 2^-76 < 2^-53). 4 DFMA in place of the ~11 FP64-pipe
+// Exact-rounding double -> float (to nearest, ties to even) on the integer
+// pipe, for results in the normal float range: rebias the exponent, keep 23
+// mantissa bits and round on the 29 dropped ones (a mantissa carry moves into
+// the exponent). Zero, float subnormals, the top float binade, Inf and NaN
+// take the hardware conversion.
+PCGB_HD float narrow(double x) {
+  unsigned lo, hi;
+  words(x, lo, hi);
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e - 897u < 253u) {
+    const unsigned long long t =
+        ((static_cast<unsigned long long>(hi & 0x7fffffffu) << 32) | lo) - (896ULL << 52);
+    unsigned f = static_cast<unsigned>(t >> 29);
+    const unsigned rem = static_cast<unsigned>(t) & 0x1fffffffu;
+    f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
+    return __uint_as_float(f | (hi & 0x80000000u));
+  }
+  return __double2float_rn(x);
+}
+
+// 1/x in FP64 from a float seed and one third-order Newton-Raphson step
+// (Markstein, IBM J. Res. Dev. 34, 1990): the seed is the float reciprocal of
+// x's truncated high word, y0 = (1 - e)/x with |e| < 2^-19.6; with
+// e = 1 - x y0, y1 = y0 (1 + e + e^2) = (1 - e^3)/x, so the remaining error
+// (< 2^-58) is below double rounding. 3 DFMA in place of the ~11 FP64-pipe
 // instructions of the correctly rounded reciprocal, within 1 ulp of it.
 // Exponents whose float seed or its reciprocal would leave the normal float
 // range (and zero, Inf, NaN) take the hardware reciprocal.
@@ -233,10 +284,9 @@ PCGB_HD double rcp64(double x) {
   const unsigned fb = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3);
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(__uint_as_float(fb)));
-  double y = widen(r);
-  y = fma(y, fma(-x, y, 1.0), y);
-  y = fma(y, fma(-x, y, 1.0), y);
-  return y;
+  const double y = widen(r);
+  const double err = fma(-x, y, 1.0);
+  return fma(y, fma(err, err, err), y);
 }
 
 // A: packed fp32 matrix (row i, column j <= i), b: fp32 right-hand side.
@@ -269,13 +319,13 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
 #pragma unroll
     for (int j = 0; j <= i; ++j) max_abs_bits(i == j ? gb : nb, c[i][j]);
   const double gam = from_bits(gb);
-  const double nu = P > 1 ? from_bits(nb) * (1.0 / sqrt(double(P * P - 1))) : 0.0;
+  const double nu = P > 1 ? from_bits(nb) * inv_sqrt_pm1_d(P) : 0.0;
   unsigned long long bb = 0x3CBCD2B297D889BCULL;  // 4e-16, solver.py:109
   if (abs_bits(gam) > bb) bb = abs_bits(gam);
   if (abs_bits(nu) > bb) bb = abs_bits(nu);
   const double inv_beta2 = rcp64(from_bits(bb));
-  const double gn = gam + nu;
-  const double delta = gn > 1.0 ? 4e-16 * gn : 4e-16;
+  const double gn = gam + nu;  // >= 0: compared with 1 on its bits
+  const double delta = abs_bits(gn) > 0x3FF0000000000000ULL ? 4e-16 * gn : 4e-16;
 
   double inv_d[P];
   double Lr[P][P];
@@ -388,7 +438,7 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
       gmw81_solve_f32in_f64<P>(A, b, x);
 #pragma unroll
       for (int k = 0; k < P; ++k) {
-        stp[k] = float(x[k]);
+        stp[k] = narrow(x[k]);
         if (!isfinite(stp[k])) stp[k] = 0.0f;
       }
     } else {
@@ -463,13 +513,19 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
         sg = fma(sd[i], widen(g[i]), sg);
       }
       const double pred = fma(-0.5, q, sg);
+      // comparisons on bit patterns (integer pipe): for positive doubles the
+      // order of the bits is the order of the values
       const long long pb = __double_as_longlong(pred);
+      const long long ab = __double_as_longlong(actual);
       const bool pzero = pb == 0;                         // +0: rho = +Inf
-      const bool pos = pb > 0;                            // > +0 (NaN has the sign bit or is > +Inf bits)
+      const bool pos = pb > 0 && pb < 0x7ff0000000000000LL;  // finite, > +0
       const bool up = f > ftp;                            // actual > 0
-      accept = up && ((pos && pb < 0x7ff0000000000000LL && actual > widen(mu) * pred) || pzero);
-      very_good = pzero || actual > widen(eta) * pred;
-      pred_neg = pred < 0.0;
+      accept = up && ((pos && ab > __double_as_longlong(widen(mu) * pred)) || pzero);
+      // only read when accept holds: then actual > 0 and pred > 0 or +0
+      very_good = pzero || ab > __double_as_longlong(widen(eta) * pred);
+      // pred < 0: sign bit set, magnitude in (0, Inf]
+      pred_neg = static_cast<unsigned long long>(pb) > 0x8000000000000000ULL &&
+                 static_cast<unsigned long long>(pb) <= 0xfff0000000000000ULL;
     } else {
       const TS actual = TS(0.5) * (TS(f) - TS(ftp));
       TS pred = TS(0);
@@ -730,7 +786,7 @@ __device__ void lm_refill(const PcgbLmParams& a, long long begin, long long end,
 }
 
 // Single-model refill kernel body: every warp starts on an empty range and
-// claims chunks of 8 items per lane from a.work. The item count may come from
+// claims chunks of items from a.work. The item count may come from
 // device memory (a compaction's counter), so the launch needs no host sync.
 template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
 __device__ void lm_refill_grid(const PcgbLmParams& a) {
@@ -739,15 +795,26 @@ __device__ void lm_refill_grid(const PcgbLmParams& a) {
     const long long d = (long long)*a.n_items_dev;
     n = d < n ? d : n;
   }
-  lm_refill<Model, M, TA, TS, SHARED_C, SHARED_B>(a, 0, 0, true, 256, n);
+  // about four chunks per warp of the grid, 32..256 items each
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  long long chunk = (n + 4 * warps - 1) / (4 * warps);
+  chunk = (chunk + 31) / 32 * 32;
+  chunk = chunk < 32 ? 32 : (chunk > 256 ? 256 : chunk);
+  lm_refill<Model, M, TA, TS, SHARED_C, SHARED_B>(a, 0, 0, true, chunk, n);
 }
 
 // Grid-stride schedule: thread t fits work items t, t + T, t + 2T, ...; an
-// item is a voxel index, or an entry of the compacted list vox_idx.
+// item is a voxel index, or an entry of the compacted list vox_idx (whose
+// length may be read from device memory, a.n_items_dev).
 template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
 __device__ void lm_grid(const PcgbLmParams& a) {
+  long long n = a.n_items;
+  if (a.n_items_dev) {
+    const long long d = (long long)*a.n_items_dev;
+    n = d < n ? d : n;
+  }
   const long long T = (long long)gridDim.x * blockDim.x;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n_items; i += T)
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += T)
     lm_fit_voxel<Model, M, TA, TS, SHARED_C, SHARED_B>(a, a.vox_idx ? (long long)a.vox_idx[i] : i);
 }
 

@@ -295,17 +295,17 @@ struct InferSmem {
   float b1[HID], b2[HID], b3[HID], b4[NOUT_PAD];
 };
 
-// pre-activations (16 voxels x 128 in 16 n8 tiles, bias included) -> GELU ->
-// bf16 A fragments of the next layer (8 k16 tiles)
+// pre-activations (16 voxels x 128 in 16 n8 tiles, bias included) -> 2 GELU ->
+// bf16 A fragments of the next layer (8 k16 tiles), whose weights are staged halved
 __device__ __forceinline__ void act_to_afrag(const float (&acc)[16][4], uint32_t (&a)[8][4]) {
 #pragma unroll
   for (int kt = 0; kt < 8; ++kt) {
     const float* lo = acc[2 * kt];
     const float* hi = acc[2 * kt + 1];
-    a[kt][0] = pack_bf16(gelu(lo[0]), gelu(lo[1]));
-    a[kt][1] = pack_bf16(gelu(lo[2]), gelu(lo[3]));
-    a[kt][2] = pack_bf16(gelu(hi[0]), gelu(hi[1]));
-    a[kt][3] = pack_bf16(gelu(hi[2]), gelu(hi[3]));
+    a[kt][0] = gelu2x_pack_bf16(lo[0], lo[1]);
+    a[kt][1] = gelu2x_pack_bf16(lo[2], lo[3]);
+    a[kt][2] = gelu2x_pack_bf16(hi[0], hi[1]);
+    a[kt][3] = gelu2x_pack_bf16(hi[2], hi[3]);
   }
 }
 
@@ -340,19 +340,19 @@ template <int NIN>
 __global__ void __launch_bounds__(384, 1) mlp_infer_kernel(const InferArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   auto& S = *reinterpret_cast<InferSmem<NIN>*>(smem_raw);
-  // stage weights and biases
+  // stage weights and biases; layers 2-4 halved, their inputs are 2 GELU
   for (int i = threadIdx.x; i < HID * (NIN + 8) / 8; i += blockDim.x) {
     const int r = i / ((NIN + 8) / 8), c = (i % ((NIN + 8) / 8)) * 8;
     *reinterpret_cast<uint4*>(&S.w1[r][c]) = *reinterpret_cast<const uint4*>(p.w[0] + r * (NIN + 8) + c);
   }
   for (int i = threadIdx.x; i < HID * LDH / 8; i += blockDim.x) {
     const int r = i / (LDH / 8), c = (i % (LDH / 8)) * 8;
-    *reinterpret_cast<uint4*>(&S.w2[r][c]) = *reinterpret_cast<const uint4*>(p.w[1] + r * LDH + c);
-    *reinterpret_cast<uint4*>(&S.w3[r][c]) = *reinterpret_cast<const uint4*>(p.w[2] + r * LDH + c);
+    *reinterpret_cast<uint4*>(&S.w2[r][c]) = halve_bf16x8(*reinterpret_cast<const uint4*>(p.w[1] + r * LDH + c));
+    *reinterpret_cast<uint4*>(&S.w3[r][c]) = halve_bf16x8(*reinterpret_cast<const uint4*>(p.w[2] + r * LDH + c));
   }
   for (int i = threadIdx.x; i < NOUT_PAD * LDH / 8; i += blockDim.x) {
     const int r = i / (LDH / 8), c = (i % (LDH / 8)) * 8;
-    *reinterpret_cast<uint4*>(&S.w4[r][c]) = *reinterpret_cast<const uint4*>(p.w[3] + r * LDH + c);
+    *reinterpret_cast<uint4*>(&S.w4[r][c]) = halve_bf16x8(*reinterpret_cast<const uint4*>(p.w[3] + r * LDH + c));
   }
   for (int i = threadIdx.x; i < HID; i += blockDim.x) {
     S.b1[i] = p.mw[0][i * (NIN + 8) + NIN];

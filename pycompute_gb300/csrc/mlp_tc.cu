@@ -13,7 +13,9 @@
 //     warpgroup and tracked by tcgen05.commit on the warpgroup's mbarrier;
 //   * the epilogue of a layer reads the accumulator row of its voxel from
 //     TMEM (tcgen05.ld 32x32b), adds the bias, applies GELU and writes the
-//     bf16 row as the next layer's A operand back into shared memory;
+//     bf16 row as the next layer's A operand back into shared memory (as
+//     2 GELU, with the next layer's weights staged halved: same products,
+//     one multiply fewer per activation);
 //   * the four warpgroups run independent tiles, so one warpgroup's MMAs
 //     overlap the other warpgroups' epilogues.
 //
@@ -159,21 +161,23 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// copy a rows x cols bf16 matrix (global leading dimension ldg) into the
-// core-matrix layout with K = kdim (columns >= cols and rows >= rows_live are zero)
-__device__ void stage_weights(bf16* dst, const bf16* src, int rows, int rows_live, int kdim, int ldg) {
+// copy a rows x kdim bf16 matrix (global leading dimension ldg) into the
+// core-matrix layout (rows >= rows_live are zero), halved when `halve` (the
+// layers after a GELU receive 2 GELU, which keeps every product unchanged)
+__device__ void stage_weights(bf16* dst, const bf16* src, int rows, int rows_live, int kdim, int ldg, bool halve) {
   const int chunks = rows * (kdim / 8);
   unsigned char* base = reinterpret_cast<unsigned char*>(dst);
   for (int c = threadIdx.x; c < chunks; c += blockDim.x) {
     const int r = c / (kdim / 8), k = (c % (kdim / 8)) * 8;
     uint4 v = make_uint4(0, 0, 0, 0);
     if (r < rows_live) v = *reinterpret_cast<const uint4*>(src + (long long)r * ldg + k);
+    if (halve) v = pcgb_mlp::halve_bf16x8(v);
     *reinterpret_cast<uint4*>(base + core_off(r, k, kdim)) = v;
   }
 }
 
-// bias + GELU of 32 accumulator columns [c0, c0 + 32), written as bf16 into
-// row r of the next layer's A operand
+// bias + 2 GELU of 32 accumulator columns [c0, c0 + 32), written as bf16
+// into row r of the next layer's A operand
 __device__ __forceinline__ void gelu_row_chunk(const float (&acc)[32], const float* bias, int c0, bf16* act, int r) {
   unsigned char* base = reinterpret_cast<unsigned char*>(act);
 #pragma unroll
@@ -183,7 +187,7 @@ __device__ __forceinline__ void gelu_row_chunk(const float (&acc)[32], const flo
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int j = q * 8 + 2 * e;
-      w[e] = pcgb_mlp::pack_bf16(pcgb_mlp::gelu(acc[j] + bias[c0 + j]), pcgb_mlp::gelu(acc[j + 1] + bias[c0 + j + 1]));
+      w[e] = pcgb_mlp::gelu2x_pack_bf16(acc[j] + bias[c0 + j], acc[j + 1] + bias[c0 + j + 1]);
     }
     *reinterpret_cast<uint4*>(base + core_off(r, c0 + q * 8, HID)) = o;
   }
@@ -197,10 +201,10 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
   const int r = (warp & 3) * 32 + lane;      // voxel row of the tile = TMEM lane
 
   // weights, biases, barriers, TMEM
-  stage_weights(S.w1, p.w[0], HID, HID, NIN, LD1_G);
-  stage_weights(S.w2, p.w[1], HID, HID, HID, LDH_G);
-  stage_weights(S.w3, p.w[2], HID, HID, HID, LDH_G);
-  stage_weights(S.w4, p.w[3], NOUT_MMA, NOUT_MAX, HID, LDH_G);
+  stage_weights(S.w1, p.w[0], HID, HID, NIN, LD1_G, false);
+  stage_weights(S.w2, p.w[1], HID, HID, HID, LDH_G, true);
+  stage_weights(S.w3, p.w[2], HID, HID, HID, LDH_G, true);
+  stage_weights(S.w4, p.w[3], NOUT_MMA, NOUT_MAX, HID, LDH_G, true);
   for (int i = threadIdx.x; i < HID; i += blockDim.x) {
     S.b1[i] = p.mw[0][i * LD1_G + NIN];
     S.b2[i] = p.mw[1][i * LDH_G + HID];

@@ -623,6 +623,7 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
     if (n_items < 0) return fail(PCGB_EINVAL, "n_items must be >= 0");
     prm.vox_idx = vox_idx;
     prm.n_items = n_items;
+    prm.n_items_dev = n_items_dev;
     return launch(ft, slot, prm, n_items, block, stream);
   }
   return launch(ft, slot, prm, nprobs, block, stream);
@@ -755,11 +756,13 @@ int pcgb_lm_run_subset(pcgb_fitter* ft, const void* consts, int64_t consts_strid
                        double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
                        void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
                        const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
-                       int block, const int32_t* vox_idx, int64_t n_items, void* stream) {
+                       int block, const int32_t* vox_idx, int64_t n_items, const uint32_t* n_items_dev,
+                       void* stream) {
+  g_err.clear();
   if (!vox_idx) return fail(PCGB_EINVAL, "vox_idx is NULL");
   return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
                      params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
-                     protocol_len, lb_host, ub_host, block, vox_idx, n_items, stream);
+                     protocol_len, lb_host, ub_host, block, vox_idx, n_items, stream, nullptr, 0, n_items_dev);
 }
 
 int pcgb_f_run_subset(pcgb_fitter* ft, const void* params, const void* consts, int64_t consts_stride,

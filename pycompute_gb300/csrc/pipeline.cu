@@ -16,11 +16,14 @@
 
 namespace pcgb_pipe {
 
-// The FP64 reciprocal used by the FP64 GMW81 solve, applied elementwise so it
-// can be checked against a correctly rounded 1/x.
-__global__ void rcp64_kernel(const double* x, double* y, long long n) {
+// The integer-pipe helpers of the FP64 GMW81 solve, applied elementwise so
+// they can be checked against correctly rounded results: rcp64(x) against 1/x,
+// narrow(x) against the double -> float conversion.
+__global__ void fp64_helpers_kernel(const double* x, double* rcp, float* nar, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) y[i] = pcgb::rcp64(x[i]);
+  if (i >= n) return;
+  if (rcp) rcp[i] = pcgb::rcp64(x[i]);
+  if (nar) nar[i] = pcgb::narrow(x[i]);
 }
 
 thread_local std::string g_err;
@@ -253,12 +256,12 @@ extern "C" {
 
 const char* pcgb_pipeline_last_error(void) { return g_err.c_str(); }
 
-int pcgb_rcp64(const double* x, double* y, int64_t n, void* stream) {
-  if (n < 0 || (n > 0 && (!x || !y))) return fail(PCGB_EINVAL, "bad rcp64 arguments");
+int pcgb_fp64_helpers(const double* x, double* rcp, float* narrowed, int64_t n, void* stream) {
+  if (n < 0 || (n > 0 && !x)) return fail(PCGB_EINVAL, "bad fp64_helpers arguments");
   if (n == 0) return PCGB_OK;
   const long long blocks = (n + 255) / 256;
-  if (blocks > 0x7fffffffLL) return fail(PCGB_ERANGE, "rcp64: n too large");
-  rcp64_kernel<<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, y, n);
+  if (blocks > 0x7fffffffLL) return fail(PCGB_ERANGE, "fp64_helpers: n too large");
+  fp64_helpers_kernel<<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(x, rcp, narrowed, n);
   return cuda_rc();
 }
 

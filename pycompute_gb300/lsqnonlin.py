@@ -387,10 +387,14 @@ class SecondOrderLevenbergMarquardt:
         return out
 
     def run_subset(self, vox_idx: torch.Tensor, n_items: int, iters: int, tol=1e-8, mu=0.25, eta=0.75, acc=0.2,
-                   dec=2.0, block: int = 0, schedule: str = "grid"):
-        """run() restricted to the voxels listed in ``vox_idx`` (int32, first n_items entries)."""
+                   dec=2.0, block: int = 0, schedule: str = "grid", n_items_dev: torch.Tensor | None = None):
+        """run() restricted to the voxels listed in ``vox_idx`` (int32, first n_items entries).
+
+        ``n_items_dev``: optional device int32 holding the list length; then
+        min(n_items_dev[0], n_items) entries are fitted without a host read.
+        """
         if schedule == "refill":
-            return self._run_refill(iters, tol, mu, eta, acc, dec, block, vox_idx, n_items)
+            return self._run_refill(iters, tol, mu, eta, acc, dec, block, vox_idx, n_items, n_items_dev=n_items_dev)
         if schedule != "grid":
             raise ValueError("schedule must be 'grid' or 'refill'")
         with torch.cuda.device(self.pars_t.device):
@@ -404,7 +408,7 @@ class SecondOrderLevenbergMarquardt:
                 _ptr(self.pars_t), _ptr(self.step_t), _ptr(self.lam_t), _ptr(self.step_type_t), _ptr(self.f_t),
                 _ptr(self.first_f), _ptr(self.last_f), _ptr(self.iters_t), self.Nprobs, int(iters), pv, plen,
                 lbh if self._bstride == 0 else None, ubh if self._bstride == 0 else None, int(block),
-                _ptr(vox_idx), int(n_items), ctypes.c_void_p(_stream_ptr()))
+                _ptr(vox_idx), int(n_items), _ptr(n_items_dev), ctypes.c_void_p(_stream_ptr()))
             _lib.check("pcgb_lm_run_subset", rc)
 
     def model_eval(self, pars_t: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:

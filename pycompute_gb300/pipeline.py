@@ -88,6 +88,7 @@ class WarmStartFitter:
         self.expr = Expr(w.expr, w.pars, w.consts)
         self._solm = None
         self._dev_consts = {}
+        self.refit_schedule = "grid"  # or "refill": schedule of the fallback refit
 
     def _fitter(self):
         if self._solm is None:
@@ -112,7 +113,7 @@ class WarmStartFitter:
         return self._buf
 
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
-            lam0: float = 1e-3, timings: dict | None = None, fused: bool = True):
+            lam0: float = 1e-3, timings: dict | None = None, fused: bool = True, events: list | None = None):
         """Warm-started fit of data (M, N); returns a WarmFit.
 
         ``fused`` (default) runs steps 3-5 as three kernels that never return
@@ -120,6 +121,9 @@ class WarmStartFitter:
         pass; the refit takes the count from device memory; cost + select in
         one pass); ``fused=False`` runs them as the separate pipeline kernels
         (cost, constant start, cost, flags, prepare, refit, cost, select).
+        ``timings`` (a dict) receives per-stage milliseconds (synchronises);
+        ``events`` (a list) receives (stage, CUDA event) pairs recorded after
+        each stage on the current stream, without synchronising.
         """
         w = self.w
         dev = data.device
@@ -129,10 +133,12 @@ class WarmStartFitter:
         ev = []
 
         def mark(name):
-            if timings is not None:
+            if timings is not None or events is not None:
                 e = torch.cuda.Event(enable_timing=True)
                 e.record()
                 ev.append((name, e))
+                if events is not None:
+                    events.append((name, e))
 
         mark("start")
         pars = self.net.infer(data, out=pars_out)
@@ -156,7 +162,7 @@ class WarmStartFitter:
                                    _p(b["backup"]), _p(b["cost_b"]), _p(b["idx"]), _p(b["counts"]), N, _stream())
             _lib.check("pcgb_warm_check", rc)
             mark("check")
-            solm._run_refill(iters_fallback, 1e-8, 0.25, 0.75, 0.2, 2.0, 0, b["idx"], N, n_items_dev=b["counts"])
+            solm.run_subset(b["idx"], N, iters_fallback, schedule=self.refit_schedule, n_items_dev=b["counts"])
             mark("refit")
             rc = L.pcgb_warm_select(prog.handle, _p(solm.consts_t), solm._cstride, _p(data), pv, plen, _p(pars),
                                     _p(b["cost"]), _p(b["backup"]), _p(b["cost_b"]), _p(b["idx"]), _p(b["counts"]),

@@ -83,8 +83,8 @@ def test_fallback_refits_flagged_voxels():
     assert np.all(cost[refit] <= c_plain.cpu().numpy()[refit] * (1 + 1e-6) + 1e-3)
 
 
-@pytest.mark.parametrize("per_voxel_bounds", [False, True])
-def test_fused_fallback_matches_separate_kernels(per_voxel_bounds):
+@pytest.mark.parametrize("per_voxel_bounds,schedule", [(False, "grid"), (True, "grid"), (False, "refill")])
+def test_fused_fallback_matches_separate_kernels(per_voxel_bounds, schedule):
     """Check + refit + select as three fused kernels (no host read of the
     flagged count) give the same fits, costs and counts as the separate
     pipeline kernels."""
@@ -93,6 +93,7 @@ def test_fused_fallback_matches_separate_kernels(per_voxel_bounds):
     out = []
     for fused in (False, True):
         wf = pipeline.WarmStartFitter(w, _BadNet(w))
+        wf.refit_schedule = schedule
         if per_voxel_bounds:
             N = data.shape[1]
             lbt = torch.tensor(w.lb, device=DEV)[:, None].expand(w.P, N).contiguous()
