@@ -324,6 +324,14 @@ const char* pcgb_noalloc_last_error(void);
 /* Last error of the pipeline entry points on this host thread. */
 const char* pcgb_pipeline_last_error(void);
 
+/* Asynchronous strided copy of `rows` rows of row_bytes bytes (pitches in
+ * bytes): a voxel range of a structure-of-arrays (rows, N) array in one call,
+ * used to stream chunks of host-resident signals and results through the GPU.
+ * direction 0 = host to device, 1 = device to host, 2 = device to device; host
+ * memory should be pinned for the copy to overlap kernels. */
+int pcgb_copy_rows_async(void* dst, int64_t dst_pitch, const void* src, int64_t src_pitch, int64_t row_bytes,
+                         int64_t rows, int direction, void* stream);
+
 /* The integer-pipe helpers of the FP64 GMW81 solve, elementwise, exposed so
  * callers and tests can check them on their own inputs: rcp[i] = 1/x[i] by a
  * float seed and one third-order Newton-Raphson step (within 1 ulp of 1/x;

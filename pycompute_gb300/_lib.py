@@ -70,6 +70,7 @@ SIGNATURES = {
     "pcgb_model_eval": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_int, c_void_p]),
     "pcgb_pipeline_last_error": (c_char_p, []),
     "pcgb_fp64_helpers": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+    "pcgb_copy_rows_async": (c_int, [c_void_p, c_i64, c_void_p, c_i64, c_i64, c_i64, c_int, c_void_p]),
     "pcgb_init_constant": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_void_p]),
     "pcgb_bpolyfit": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_i64, c_int, c_int, c_int, c_int, c_void_p,
                               c_void_p]),
@@ -135,7 +136,7 @@ def check(fn_name: str, rc: int):
             err = L.pcgb_mlp_last_error
         elif fn_name.startswith("pcgb_multi_run_noalloc"):
             err = L.pcgb_noalloc_last_error
-        elif fn_name.startswith(("pcgb_init_constant", "pcgb_fp64_helpers", "pcgb_fallback", "pcgb_bpolyfit", "pcgb_ivim")):
+        elif fn_name.startswith(("pcgb_init_constant", "pcgb_fp64_helpers", "pcgb_copy_rows", "pcgb_fallback", "pcgb_bpolyfit", "pcgb_ivim")):
             err = L.pcgb_pipeline_last_error
         else:
             err = L.pcgb_last_error

@@ -256,6 +256,24 @@ extern "C" {
 
 const char* pcgb_pipeline_last_error(void) { return g_err.c_str(); }
 
+int pcgb_copy_rows_async(void* dst, int64_t dst_pitch, const void* src, int64_t src_pitch, int64_t row_bytes,
+                         int64_t rows, int direction, void* stream) {
+  if (rows < 0 || row_bytes < 0 || dst_pitch < row_bytes || src_pitch < row_bytes)
+    return fail(PCGB_EINVAL, "copy_rows: pitches must cover row_bytes, sizes >= 0");
+  if (rows == 0 || row_bytes == 0) return PCGB_OK;
+  if (!dst || !src) return fail(PCGB_EINVAL, "copy_rows: null pointer");
+  cudaMemcpyKind kind;
+  switch (direction) {
+    case 0: kind = cudaMemcpyHostToDevice; break;
+    case 1: kind = cudaMemcpyDeviceToHost; break;
+    case 2: kind = cudaMemcpyDeviceToDevice; break;
+    default: return fail(PCGB_EINVAL, "copy_rows: direction must be 0 (H2D), 1 (D2H) or 2 (D2D)");
+  }
+  const cudaError_t e = cudaMemcpy2DAsync(dst, size_t(dst_pitch), src, size_t(src_pitch), size_t(row_bytes),
+                                          size_t(rows), kind, static_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? PCGB_OK : fail(PCGB_ECUDA, cudaGetErrorString(e));
+}
+
 int pcgb_fp64_helpers(const double* x, double* rcp, float* narrowed, int64_t n, void* stream) {
   if (n < 0 || (n > 0 && !x)) return fail(PCGB_EINVAL, "bad fp64_helpers arguments");
   if (n == 0) return PCGB_OK;

@@ -101,6 +101,71 @@ class WarmStartFitter:
         w = self.w
         return list(w.protocol), list(w.lb), list(w.ub)
 
+    def fit_host(self, data_h: torch.Tensor, out_h: torch.Tensor, iters_warm: int, iters_fallback: int,
+                 lam0: float = 1e-3, chunks: int = 8, device=None) -> torch.Tensor:
+        """Warm-started fit of host-resident signals, streamed through the GPU.
+
+        data_h (M, N) and out_h (P, N) are float32 host tensors (pinned, so the
+        copies overlap the fits). The voxels go through in ``chunks`` ranges:
+        chunk c is copied in on one stream while chunk c-1 is fitted on
+        another and chunk c-2's parameters are copied back on a third; every
+        voxel's result equals fit()'s. Returns the device int32 tensor
+        [fallback voxels, refits kept] summed over chunks. Work is ordered
+        after the caller's current stream, and the caller's stream waits for
+        the last copy back.
+        """
+        M, N = data_h.shape
+        P = self.w.P
+        if tuple(out_h.shape) != (P, N) or data_h.dtype != torch.float32 or out_h.dtype != torch.float32:
+            raise ValueError("data_h must be (M, N) and out_h (P, N) float32")
+        dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        chunks = max(1, min(int(chunks), (N + 127) // 128))
+        n_c = (N + chunks - 1) // chunks
+        n_c = (n_c + 127) // 128 * 128
+        nchunk = (N + n_c - 1) // n_c
+        slots = 2
+        key = (M, P, n_c, str(dev))
+        if getattr(self, "_host_key", None) != key:
+            self._host = dict(data=[torch.empty(M * n_c, dtype=torch.float32, device=dev) for _ in range(slots)],
+                              pars=[torch.empty(P * n_c, dtype=torch.float32, device=dev) for _ in range(slots)],
+                              streams=[torch.cuda.Stream(device=dev) for _ in range(3)])
+            self._host_key = key
+        hb = self._host
+        s_in, s_fit, s_out = hb["streams"]
+        caller = torch.cuda.current_stream(dev)
+        for st in (s_in, s_fit, s_out):
+            st.wait_stream(caller)
+        total = torch.zeros(2, dtype=torch.int32, device=dev)
+        total.record_stream(s_fit)
+        ev_in = [torch.cuda.Event() for _ in range(nchunk)]
+        ev_fit = [torch.cuda.Event() for _ in range(nchunk)]
+        ev_out = [torch.cuda.Event() for _ in range(nchunk)]
+        for c in range(nchunk):
+            lo = c * n_c
+            n = min(N, lo + n_c) - lo
+            k = c % slots
+            d = hb["data"][k][:M * n].view(M, n)
+            p = hb["pars"][k][:P * n].view(P, n)
+            with torch.cuda.stream(s_in):
+                if c >= slots:
+                    s_in.wait_event(ev_fit[c - slots])  # the slot's signals are no longer read
+                copy_rows(d, 0, data_h, lo, n)
+                ev_in[c].record(s_in)
+            with torch.cuda.stream(s_fit):
+                s_fit.wait_event(ev_in[c])
+                if c >= slots:
+                    s_fit.wait_event(ev_out[c - slots])  # the slot's parameters are copied out
+                res = self.fit(d, iters_warm, iters_fallback, pars_out=p, lam0=lam0)
+                total.add_(res.counts)
+                ev_fit[c].record(s_fit)
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(ev_fit[c])
+                copy_rows(out_h, lo, p, 0, n)
+                ev_out[c].record(s_out)
+        caller.wait_stream(s_fit)
+        caller.wait_stream(s_out)
+        return total
+
     def _buffers(self, P: int, N: int, dev):
         key = (P, N, str(dev))
         if getattr(self, "_buf_key", None) != key:
@@ -209,6 +274,22 @@ class WarmStartFitter:
             for (n0, e0), (n1, e1) in zip(ev[:-1], ev[1:]):
                 timings[n1] = timings.get(n1, 0.0) + e0.elapsed_time(e1)
         return WarmFit(pars, cost, torch.tensor([nfb, kept_refit], dtype=torch.int32), solm.step_type_t)
+
+
+def copy_rows(dst: torch.Tensor, dst_col: int, src: torch.Tensor, src_col: int, ncols: int):
+    """dst[:, dst_col:dst_col+ncols] = src[:, src_col:src_col+ncols] for 2-D float32
+    row-major tensors (host or device), asynchronously on the current stream."""
+    rows = src.shape[0]
+    if dst.shape[0] != rows or dst.dtype != src.dtype or not (dst.is_contiguous() and src.is_contiguous()):
+        raise ValueError("copy_rows needs contiguous 2-D tensors of the same dtype and row count")
+    es = src.element_size()
+    direction = 0 if (dst.is_cuda and not src.is_cuda) else (1 if (src.is_cuda and not dst.is_cuda) else 2)
+    if not dst.is_cuda and not src.is_cuda:
+        raise ValueError("copy_rows copies to or from the device")
+    rc = _lib.lib().pcgb_copy_rows_async(ctypes.c_void_p(dst.data_ptr() + dst_col * es), dst.stride(0) * es,
+                                         ctypes.c_void_p(src.data_ptr() + src_col * es), src.stride(0) * es,
+                                         ncols * es, rows, direction, _stream())
+    _lib.check("pcgb_copy_rows_async", rc)
 
 
 class WarmFit:

@@ -109,6 +109,26 @@ def test_fused_fallback_matches_separate_kernels(per_voxel_bounds, schedule):
     np.testing.assert_array_equal(c0, c1)
 
 
+@pytest.mark.parametrize("N,chunks", [(100003, 3), (65536, 8), (1000, 4)])
+def test_fit_host_streams_chunks_with_fit_results(N, chunks):
+    """fit_host (chunked copies overlapping the fits) gives every voxel the
+    result of one device-resident fit() of all voxels."""
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    true, data = pipeline.synth_gpu(w, N, seed=12, device=DEV)
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, DEV, seed=5)  # untrained: a per-voxel start all the same
+    net.fit_normalisation(data, true)
+    wf = pipeline.WarmStartFitter(w, net)
+    ref = wf.fit(data, iters_warm=3, iters_fallback=20)
+    torch.cuda.synchronize()
+    p_ref, n_ref = ref.pars.cpu().numpy().copy(), ref.n_fallback
+    data_h = data.cpu().pin_memory()
+    out_h = torch.full((w.P, N), float("nan")).pin_memory()
+    counts = wf.fit_host(data_h, out_h, iters_warm=3, iters_fallback=20, chunks=chunks)
+    torch.cuda.synchronize()
+    np.testing.assert_array_equal(out_h.numpy(), p_ref)
+    assert int(counts[0]) == n_ref
+
+
 def test_trained_network_beats_plain_lm_at_equal_iterations():
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     # training set: signals and the plain LM's fits of them as labels
