@@ -173,6 +173,34 @@ int pcgb_warm_check(pcgb_fitter* fitter, const void* consts, int64_t consts_stri
                     int64_t nprobs, void* stream);
 
 /*
+ * pcgb_lm_run with pcgb_warm_check as its epilogue, in one launch: the check
+ * runs on the samples and the fit still in registers (no second pass over the
+ * signals). Arguments as in pcgb_lm_run followed by those of pcgb_warm_check;
+ * results equal pcgb_lm_run then pcgb_warm_check. No reference counterpart.
+ */
+int pcgb_lm_run_check(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                      const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                      double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                      void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                      const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                      int block, const double* init_values, double lam0, void* cost, void* pars_backup,
+                      void* cost_backup, int32_t* fb_idx, uint32_t* fb_count, void* stream);
+
+/*
+ * The refit of the fb_count[0] flagged voxels of fb_idx (as pcgb_lm_run_subset
+ * with n_items_dev = fb_count) with pcgb_warm_select as its epilogue, in one
+ * launch. Results equal the subset run followed by pcgb_warm_select. No
+ * reference counterpart.
+ */
+int pcgb_lm_run_select(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                       void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                       const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                       int block, void* cost, const void* pars_backup, const void* cost_backup,
+                       const int32_t* fb_idx, uint32_t* fb_count, int8_t* which, void* stream);
+
+/*
  * After the refit of the flagged voxels: for each of the fb_count[0] voxels of
  * fb_idx, the cost at its refitted params is compared with cost_backup; the
  * lower fit is kept in params and cost, fb_count[1] counts the kept refits,

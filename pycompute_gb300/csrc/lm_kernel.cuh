@@ -698,6 +698,14 @@ struct VoxelFit {
     return true;
   }
 
+  // parameters and samples only (for a voxel converged before the call)
+  PCGB_HD void load_fit(const PcgbLmParams& a, long long v) {
+#pragma unroll
+    for (int k = 0; k < P; ++k) p[k] = load_<TA>(a.pars, k * a.N + v);
+#pragma unroll
+    for (int i = 0; i < M; ++i) d[i] = load_<TA>(a.data, i * a.N + v);
+  }
+
   PCGB_HD bool finished(const PcgbLmParams& a) const { return st == 0 || it >= a.iters; }
 
   PCGB_HD void step(const PcgbLmParams& a) {
@@ -891,13 +899,15 @@ __device__ void eval_grid(const PcgbLmParams& a) {
 //
 // A warm-started fit is refitted from the plain fitter's constant start where
 // its cost is not finite, not below the cost at that start, or where it ends
-// on a bound. warm_check_grid decides this for every voxel in one pass over
-// its samples (both costs from registers), compacts the flagged voxels with
-// one atomic per warp, saves their warm fits and resets their fitter state to
-// the constant start. The refit then runs on the compacted list with the
-// count read from device memory, and warm_select_grid keeps, per flagged
-// voxel, whichever of the two fits has the lower cost. No step needs the
-// flagged count on the host.
+// on a bound. The check decides this per voxel from registers (both costs),
+// compacts the flagged voxels with one atomic per warp, saves their warm fits
+// and resets their fitter state to the constant start; the refit runs on the
+// compacted list with the count read from device memory, and the select keeps,
+// per flagged voxel, whichever of the two fits has the lower cost. No step
+// needs the flagged count on the host. The check runs either as its own pass
+// (warm_check_grid) or as the epilogue of the warm LM (lm_check_grid), the
+// select as its own pass (warm_select_grid) or as the epilogue of the refit
+// (lm_select_grid).
 
 // sum_i (m(p; c_i) - d_i)^2, in the order of cost_grid
 template <class Model, int M, typename TA, class CF>
@@ -928,27 +938,23 @@ PCGB_HD TA voxel_cost(const PcgbLmParams& a, long long v, const TA (&p)[Model::P
   }
 }
 
-// one thread per voxel, grid covering N (every lane reaches the ballot)
+// The check of one voxel from its warm fit p and samples d in registers
+// (valid = the lane has a voxel; every lane of the warp calls this, for the
+// ballot): cost at p into a.cost, flag, compaction into a.fb_idx, backup of
+// the warm fit, state reset to the constant start.
 template <class Model, int M, typename TA, bool SHARED_C>
-__device__ void warm_check_grid(const PcgbLmParams& a) {
+__device__ void warm_check_voxel(const PcgbLmParams& a, long long v, bool valid, const TA (&p)[Model::P],
+                                 const TA (&d)[M]) {
   constexpr int P = Model::P;
   const long long N = a.N;
-  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   bool flag = false;
-  TA p[P], p0[P], c = TA(0);
-  if (v < N) {
-    TA d[M];
+  TA p0[P], c = TA(0);
+  if (valid) {
     TA mx = -Num<TA>::inf();
 #pragma unroll
-    for (int i = 0; i < M; ++i) {
-      d[i] = load<TA>(a.data, i * N + v);
-      mx = fmax(mx, d[i]);
-    }
+    for (int i = 0; i < M; ++i) mx = fmax(mx, d[i]);
 #pragma unroll
-    for (int k = 0; k < P; ++k) {
-      p[k] = load<TA>(a.pars, k * N + v);
-      p0[k] = isnan(a.init_val[k]) ? mx : TA(a.init_val[k]);
-    }
+    for (int k = 0; k < P; ++k) p0[k] = isnan(a.init_val[k]) ? mx : TA(a.init_val[k]);
     c = voxel_cost<Model, M, TA, SHARED_C>(a, v, p, d);
     const TA c0 = voxel_cost<Model, M, TA, SHARED_C>(a, v, p0, d);
     flag = !isfinite(c) || !(c < c0);
@@ -980,16 +986,78 @@ __device__ void warm_check_grid(const PcgbLmParams& a) {
   static_cast<TA*>(a.f)[v] = TA(0);
 }
 
-// grid-stride over the flagged voxels (count from a.n_items_dev)
+// one thread per voxel, grid covering N (every lane reaches the ballot)
 template <class Model, int M, typename TA, bool SHARED_C>
-__device__ void warm_select_grid(const PcgbLmParams& a) {
+__device__ void warm_check_grid(const PcgbLmParams& a) {
   constexpr int P = Model::P;
   const long long N = a.N;
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  TA p[P], d[M];
+  if (v < N) {
+#pragma unroll
+    for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
+#pragma unroll
+    for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * N + v);
+  }
+  warm_check_voxel<Model, M, TA, SHARED_C>(a, v, v < N, p, d);
+}
+
+// The warm LM with the check as its epilogue: the samples and the fit are
+// still in registers when the iterations end, so the check costs two model
+// evaluations and no second pass over the signals. One thread per voxel,
+// grid covering N. Per voxel the same arithmetic as lm_grid + warm_check_grid.
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+__device__ void lm_check_grid(const PcgbLmParams& a) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = v < a.N;
+  VoxelFit<Model, M, TA, TS, SHARED_C, SHARED_B> s;
+  if (valid) {
+    if (s.load(a, v)) {
+      while (!s.finished(a)) s.step(a);
+      s.store(a, v);
+    } else {
+      s.load_fit(a, v);  // converged before the call: the check still needs p and d
+    }
+  }
+  warm_check_voxel<Model, M, TA, SHARED_C>(a, v, valid, s.p, s.d);
+}
+
+// keep the refit or restore the warm fit of flagged item i (voxel v), from
+// the refit's parameters and samples in registers
+template <class Model, int M, typename TA, bool SHARED_C>
+__device__ void warm_select_voxel(const PcgbLmParams& a, long long i, long long v, const TA (&p)[Model::P],
+                                  const TA (&d)[M]) {
+  constexpr int P = Model::P;
+  const long long N = a.N;
+  const TA c = voxel_cost<Model, M, TA, SHARED_C>(a, v, p, d);
+  const TA cb = load<TA>(a.cost_backup, i);
+  const bool refit = c < cb;
+  if (!refit) {
+#pragma unroll
+    for (int k = 0; k < P; ++k) static_cast<TA*>(a.pars)[k * N + v] = load<TA>(a.pars_backup, k * N + i);
+  }
+  static_cast<TA*>(a.cost)[v] = refit ? c : cb;
+  if (a.which) a.which[v] = refit ? 1 : 0;
+  const unsigned m = __activemask();
+  const unsigned kept = __ballot_sync(m, refit);
+  if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1) && kept) atomicAdd(a.fb_count + 1, (unsigned)__popc(kept));
+}
+
+PCGB_HD long long device_count(const PcgbLmParams& a) {
   long long n = a.n_items;
   if (a.n_items_dev) {
     const long long d = (long long)*a.n_items_dev;
     n = d < n ? d : n;
   }
+  return n;
+}
+
+// grid-stride over the flagged voxels (count from a.n_items_dev)
+template <class Model, int M, typename TA, bool SHARED_C>
+__device__ void warm_select_grid(const PcgbLmParams& a) {
+  constexpr int P = Model::P;
+  const long long N = a.N;
+  const long long n = device_count(a);
   const long long T = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += T) {
     const long long v = a.fb_idx[i];
@@ -997,19 +1065,27 @@ __device__ void warm_select_grid(const PcgbLmParams& a) {
 #pragma unroll
     for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * N + v);
 #pragma unroll
-    for (int s = 0; s < M; ++s) d[s] = load<TA>(a.data, s * N + v);
-    const TA c = voxel_cost<Model, M, TA, SHARED_C>(a, v, p, d);
-    const TA cb = load<TA>(a.cost_backup, i);
-    const bool refit = c < cb;
-    if (!refit) {
-#pragma unroll
-      for (int k = 0; k < P; ++k) static_cast<TA*>(a.pars)[k * N + v] = load<TA>(a.pars_backup, k * N + i);
+    for (int q = 0; q < M; ++q) d[q] = load<TA>(a.data, q * N + v);
+    warm_select_voxel<Model, M, TA, SHARED_C>(a, i, v, p, d);
+  }
+}
+
+// The refit of the flagged voxels with the select as its epilogue
+// (grid-stride over the compacted list, count from a.n_items_dev).
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+__device__ void lm_select_grid(const PcgbLmParams& a) {
+  const long long n = device_count(a);
+  const long long T = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += T) {
+    const long long v = a.vox_idx[i];
+    VoxelFit<Model, M, TA, TS, SHARED_C, SHARED_B> s;
+    if (s.load(a, v)) {
+      while (!s.finished(a)) s.step(a);
+      s.store(a, v);
+    } else {
+      s.load_fit(a, v);
     }
-    static_cast<TA*>(a.cost)[v] = refit ? c : cb;
-    if (a.which) a.which[v] = refit ? 1 : 0;
-    const unsigned m = __activemask();
-    const unsigned kept = __ballot_sync(m, refit);
-    if ((threadIdx.x & 31u) == (unsigned)(__ffs(m) - 1) && kept) atomicAdd(a.fb_count + 1, (unsigned)__popc(kept));
+    warm_select_voxel<Model, M, TA, SHARED_C>(a, i, v, s.p, s.d);
   }
 }
 

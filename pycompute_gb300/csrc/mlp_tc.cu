@@ -6,18 +6,20 @@
 //
 //   * one CTA per SM, 16 warps = 4 warpgroups; each warpgroup owns one
 //     128-voxel tile at a time (thread t of the warpgroup = voxel t = TMEM
-//     lane t) and its own 128 TMEM columns for the layer accumulator;
+//     lane t) and its own 128 TMEM columns for the layer accumulator, and
+//     loads the next tile's signals while it works on the current one;
 //   * a layer is D[128 x N] = A[128 x K] * W^T with A (activations) and W
 //     (weights, N x K) in shared memory, issued as K/16 tcgen05.mma
 //     (kind::f16, bf16 x bf16 -> f32, M = 128) by one thread of the
 //     warpgroup and tracked by tcgen05.commit on the warpgroup's mbarrier;
-//   * the epilogue of a layer reads the accumulator row of its voxel from
-//     TMEM (tcgen05.ld 32x32b), adds the bias, applies GELU and writes the
-//     bf16 row as the next layer's A operand back into shared memory (as
-//     2 GELU, with the next layer's weights staged halved: same products,
-//     one multiply fewer per activation);
-//   * the four warpgroups run independent tiles, so one warpgroup's MMAs
-//     overlap the other warpgroups' epilogues.
+//   * the bias enters the accumulator through one more MMA per layer (see
+//     TcSmem), so the epilogue reads the pre-activation row of its voxel from
+//     TMEM (tcgen05.ld 32x32b), applies GELU and writes the bf16 row as the
+//     next layer's A operand back into shared memory (as 2 GELU, with the
+//     next layer's weights staged halved: same products, one multiply fewer
+//     per activation);
+//   * the warpgroups run independent tiles, so one warpgroup's MMAs overlap
+//     the other warpgroups' epilogues.
 //
 // Shared-memory operands use the canonical K-major layout without swizzle:
 // 8 x 16-byte core matrices (8 rows x 8 bf16), element (r, k) of an R x K
@@ -44,19 +46,27 @@ constexpr int NOUT_MMA = 16;  // the last layer's N (>= P, multiple of 16)
 constexpr int NOUT_MAX = 8;
 constexpr int NWG = 4;        // warpgroups (tiles in flight) per CTA
 constexpr int THREADS = NWG * 128;
-constexpr int TMEM_COLS = 512;  // NWG x 128 accumulator columns
+constexpr int TMEM_COLS = 512;  // >= NWG x 128 accumulator columns, a power of 2
 constexpr int LDH_G = HID + 8;  // leading dimension of the hidden weights in global memory
 constexpr int LD1_G = NIN + 8;  // ... of the first layer's weights
 constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait counts as lost
 
+// The biases enter the accumulators through one more MMA per layer: A = a
+// 128 x 16 tile whose first two columns are 1, B = the layer's bias split
+// into two bf16 terms (b_hi = bf16(b), b_lo = bf16(b - b_hi): b to 2^-16
+// relative) in its first two columns. The epilogue then has no bias add.
 struct __align__(1024) TcSmem {
   bf16 w1[HID * NIN];
   bf16 w2[HID * HID];
   bf16 w3[HID * HID];
   bf16 w4[NOUT_MMA * HID];
-  bf16 x[NWG][128 * NIN];
+  bf16 bias[3][HID * 16];   // B operands of the bias MMAs of layers 1-3
+  bf16 bias4[NOUT_MMA * 16];
+  bf16 ones[128 * 16];      // A operand of the bias MMAs
+  // per warpgroup: the layer-1 input tile (128 x 16) at the start of its
+  // activation tile (128 x 128); the first epilogue overwrites it only after
+  // the layer-1 MMAs that read it have completed
   bf16 act[NWG][128 * HID];
-  float b1[HID], b2[HID], b3[HID], b4[NOUT_MMA];
   unsigned long long mbar[NWG];
   uint32_t tmem_base;
 };
@@ -134,9 +144,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
   return false;
 }
 
-// 32 consecutive fp32 accumulator columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
+// Start loading 32 consecutive fp32 accumulator columns of this thread's TMEM
+// lane; the registers are valid only after tmem_wait32 on the same array.
+__device__ __forceinline__ void tmem_ld32_start(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
       "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
@@ -145,9 +155,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
         "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
         "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+// Wait for every outstanding tcgen05.ld of this thread; the registers of r are
+// read-write operands, so no use of them can be scheduled before the wait.
+__device__ __forceinline__ void tmem_wait32(uint32_t (&r)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                 "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                 "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+               :
+               : "memory");
 }
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
@@ -176,9 +195,9 @@ __device__ void stage_weights(bf16* dst, const bf16* src, int rows, int rows_liv
   }
 }
 
-// bias + 2 GELU of 32 accumulator columns [c0, c0 + 32), written as bf16
-// into row r of the next layer's A operand
-__device__ __forceinline__ void gelu_row_chunk(const float (&acc)[32], const float* bias, int c0, bf16* act, int r) {
+// 2 GELU of 32 pre-activations (columns [c0, c0 + 32), bias included), written
+// as bf16 into row r of the next layer's A operand
+__device__ __forceinline__ void gelu_row_chunk(const uint32_t (&acc)[32], int c0, bf16* act, int r) {
   unsigned char* base = reinterpret_cast<unsigned char*>(act);
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
@@ -187,9 +206,26 @@ __device__ __forceinline__ void gelu_row_chunk(const float (&acc)[32], const flo
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int j = q * 8 + 2 * e;
-      w[e] = pcgb_mlp::gelu2x_pack_bf16(acc[j] + bias[c0 + j], acc[j + 1] + bias[c0 + j + 1]);
+      w[e] = pcgb_mlp::gelu2x_pack_bf16(__uint_as_float(acc[j]), __uint_as_float(acc[j + 1]));
     }
     *reinterpret_cast<uint4*>(base + core_off(r, c0 + q * 8, HID)) = o;
+  }
+}
+
+// B operand (rows x 16, core-matrix layout) of a bias MMA: columns 0 and 1 hold
+// the two bf16 terms of each row's fp32 bias, the rest is zero
+__device__ void stage_bias(bf16* dst, const float* master, int rows, int rows_live, int ld, int col) {
+  unsigned char* base = reinterpret_cast<unsigned char*>(dst);
+  for (int c = threadIdx.x; c < rows * 2; c += blockDim.x) {
+    const int r = c >> 1, k = (c & 1) * 8;
+    uint4 v = make_uint4(0, 0, 0, 0);
+    if (k == 0 && r < rows_live) {
+      const float b = master[(long long)r * ld + col];
+      const bf16 hi = __float2bfloat16_rn(b);
+      const bf16 lo = __float2bfloat16_rn(b - __bfloat162float(hi));
+      v.x = uint32_t(__bfloat16_as_ushort(hi)) | (uint32_t(__bfloat16_as_ushort(lo)) << 16);
+    }
+    *reinterpret_cast<uint4*>(base + core_off(r, k, 16)) = v;
   }
 }
 
@@ -205,12 +241,16 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
   stage_weights(S.w2, p.w[1], HID, HID, HID, LDH_G, true);
   stage_weights(S.w3, p.w[2], HID, HID, HID, LDH_G, true);
   stage_weights(S.w4, p.w[3], NOUT_MMA, NOUT_MAX, HID, LDH_G, true);
-  for (int i = threadIdx.x; i < HID; i += blockDim.x) {
-    S.b1[i] = p.mw[0][i * LD1_G + NIN];
-    S.b2[i] = p.mw[1][i * LDH_G + HID];
-    S.b3[i] = p.mw[2][i * LDH_G + HID];
+  stage_bias(S.bias[0], p.mw[0], HID, HID, LD1_G, NIN);
+  stage_bias(S.bias[1], p.mw[1], HID, HID, LDH_G, HID);
+  stage_bias(S.bias[2], p.mw[2], HID, HID, LDH_G, HID);
+  stage_bias(S.bias4, p.mw[3], NOUT_MMA, NOUT_MAX, LDH_G, HID);
+  for (int c = threadIdx.x; c < 128 * 2; c += blockDim.x) {
+    const int r = c >> 1, k = (c & 1) * 8;
+    const uint32_t one2 = 0x3F803F80u;  // two bf16 ones
+    const uint4 v = k == 0 ? make_uint4(one2, 0, 0, 0) : make_uint4(0, 0, 0, 0);
+    *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.ones) + core_off(r, k, 16)) = v;
   }
-  if (threadIdx.x < NOUT_MMA) S.b4[threadIdx.x] = threadIdx.x < NOUT_MAX ? p.mw[3][threadIdx.x * LDH_G + HID] : 0.f;
   if (threadIdx.x == 0) {
     for (int i = 0; i < NWG; ++i)
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.mbar[i])) : "memory");
@@ -231,29 +271,42 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
   const uint32_t d_tmem = tbase + uint32_t(g * 128);                           // lane 0, this warpgroup's columns
   const uint32_t t_row = tbase + (uint32_t((warp & 3) * 32) << 16) + uint32_t(g * 128);  // this warp's lanes
   const uint32_t mbar = smem_u32(&S.mbar[g]);
-  const uint32_t xs = smem_u32(S.x[g]), as = smem_u32(S.act[g]);
+  const uint32_t xs = smem_u32(S.act[g]), as = smem_u32(S.act[g]);
   const uint32_t w1s = smem_u32(S.w1), w2s = smem_u32(S.w2), w3s = smem_u32(S.w3), w4s = smem_u32(S.w4);
+  const uint32_t ones_s = smem_u32(S.ones);
   const bool issuer = r == 0;
   constexpr uint32_t ID_HID = idesc_bf16(128, HID), ID_OUT = idesc_bf16(128, NOUT_MMA);
   uint32_t phase = 0;
   bool lost = false;
 
   const long long ntiles = (p.n + 127) / 128;
-  for (long long tile = (long long)blockIdx.x * NWG + g; tile < ntiles && !lost;
-       tile += (long long)gridDim.x * NWG) {
+  const long long tstride = (long long)gridDim.x * NWG;
+  // signals of the next tile, loaded one tile ahead of their use
+  float s_next[NIN];
+  {
+    const long long v0 = ((long long)blockIdx.x * NWG + g) * 128 + r;
+#pragma unroll
+    for (int k = 0; k < NIN; ++k) s_next[k] = v0 < p.n ? p.signals[(long long)k * p.n + v0] : 0.f;
+  }
+  for (long long tile = (long long)blockIdx.x * NWG + g; tile < ntiles && !lost; tile += tstride) {
     const long long v = tile * 128 + r;
     // ---- inputs: 16 samples of voxel v -> bf16 row r of x
     float s[NIN];
     float mx = 0.f;
 #pragma unroll
     for (int k = 0; k < NIN; ++k) {
-      s[k] = v < p.n ? p.signals[(long long)k * p.n + v] : 0.f;
+      s[k] = s_next[k];
       mx = fmaxf(mx, s[k]);
+    }
+    {
+      const long long vn = v + tstride * 128;
+#pragma unroll
+      for (int k = 0; k < NIN; ++k) s_next[k] = vn < p.n ? p.signals[(long long)k * p.n + vn] : 0.f;
     }
     mx = fmaxf(mx, 1e-20f);
     const float inv = 1.f / mx;
     {
-      unsigned char* xb = reinterpret_cast<unsigned char*>(S.x[g]);
+      unsigned char* xb = reinterpret_cast<unsigned char*>(S.act[g]);
 #pragma unroll
       for (int q = 0; q < 2; ++q) {
         uint4 o;
@@ -282,6 +335,9 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
             mma_bf16(d_tmem, smem_desc(as + kk * 256, 128, 2048), smem_desc(ws + kk * 256, 128, 2048), id,
                      kk > 0 ? 1u : 0u);
         }
+        // + bias: ones (128 x 16) times the layer's bias terms (N x 16)
+        const uint32_t bs = layer < 3 ? smem_u32(S.bias[layer]) : smem_u32(S.bias4);
+        mma_bf16(d_tmem, smem_desc(ones_s, 128, 256), smem_desc(bs, 128, 256), layer == 3 ? ID_OUT : ID_HID, 1u);
         mma_commit(mbar);
       }
       const bool ok = mbar_wait(mbar, phase);
@@ -292,12 +348,12 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
       }
       fence_after_sync();
       if (layer < 3) {
-        const float* bias = layer == 0 ? S.b1 : (layer == 1 ? S.b2 : S.b3);
 #pragma unroll 1
         for (int c = 0; c < HID / 32; ++c) {
-          float acc[32];
-          tmem_ld32(t_row + uint32_t(c * 32), acc);
-          gelu_row_chunk(acc, bias, c * 32, S.act[g], r);
+          uint32_t acc[32];
+          tmem_ld32_start(t_row + uint32_t(c * 32), acc);
+          tmem_wait32(acc);
+          gelu_row_chunk(acc, c * 32, S.act[g], r);
         }
       } else {
         float y[16];
@@ -306,7 +362,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
 #pragma unroll
           for (int k = 0; k < NOUT_MAX; ++k) {
             if (k >= p.nout) break;
-            const float t = (y[k] + S.b4[k]) * p.stdv[k] + p.mean[k];
+            const float t = y[k] * p.stdv[k] + p.mean[k];
             const int kind = p.kinds[k];
             float val = kind == 0 ? t * mx : (kind == 2 ? expf(t) : t);
             val = fminf(fmaxf(val, p.lb[k]), p.ub[k]);

@@ -56,14 +56,17 @@ uint64_t fnv1a(const std::string& s, uint64_t h = 1469598103934665603ull) {
 enum KernelSlot {
   K_LM_C1_B1, K_LM_C1_B0, K_LM_C0_B1, K_LM_C0_B0, K_COST_C1, K_COST_C0, K_GMW, K_EVAL_C1, K_EVAL_C0,
   K_SEARCH_C1, K_SEARCH_C0, K_RS_C1_B1, K_RS_C1_B0, K_RS_C0_B1, K_RS_C0_B0,
-  K_LMQ_C1_B1, K_LMQ_C1_B0, K_LMQ_C0_B1, K_LMQ_C0_B0, K_CHECK_C1, K_CHECK_C0, K_SELECT_C1, K_SELECT_C0, K_COUNT
+  K_LMQ_C1_B1, K_LMQ_C1_B0, K_LMQ_C0_B1, K_LMQ_C0_B0, K_CHECK_C1, K_CHECK_C0, K_SELECT_C1, K_SELECT_C0,
+  K_LMC_C1_B1, K_LMC_C1_B0, K_LMC_C0_B1, K_LMC_C0_B0, K_LMS_C1_B1, K_LMS_C1_B0, K_LMS_C0_B1, K_LMS_C0_B0, K_COUNT
 };
 const char* kKernelNames[K_COUNT] = {"pcgb_lm_c1_b1", "pcgb_lm_c1_b0", "pcgb_lm_c0_b1", "pcgb_lm_c0_b0",
                                      "pcgb_cost_c1",  "pcgb_cost_c0",  "pcgb_gmw81",    "pcgb_eval_c1",
                                      "pcgb_eval_c0",  "pcgb_search_c1", "pcgb_search_c0", "pcgb_rs_c1_b1",
                                      "pcgb_rs_c1_b0", "pcgb_rs_c0_b1", "pcgb_rs_c0_b0", "pcgb_lmq_c1_b1",
                                      "pcgb_lmq_c1_b0", "pcgb_lmq_c0_b1", "pcgb_lmq_c0_b0", "pcgb_check_c1",
-                                     "pcgb_check_c0", "pcgb_select_c1", "pcgb_select_c0"};
+                                     "pcgb_check_c0", "pcgb_select_c1", "pcgb_select_c0", "pcgb_lmc_c1_b1",
+                                     "pcgb_lmc_c1_b0", "pcgb_lmc_c0_b1", "pcgb_lmc_c0_b0", "pcgb_lms_c1_b1",
+                                     "pcgb_lms_c1_b0", "pcgb_lms_c0_b1", "pcgb_lms_c0_b0"};
 
 constexpr int kDefaultBlock = 128;
 constexpr int kMaxBlock = 256;
@@ -73,49 +76,80 @@ constexpr int kMaxBlock = 256;
 struct pcgb_fitter {
   int P = 0, C = 0, M = 0, dtype = 0, sdtype = 0;
   int device = -1;
-  cudaLibrary_t lib = nullptr;
+  cudaLibrary_t lib[3] = {};  // one per kernel group, loaded on first use
   cudaKernel_t k[K_COUNT] = {};
+  std::string source, structname, cache_dir;
+  std::mutex mu;
   std::string log;
 };
 
 namespace {
 
+// Kernel groups, each its own NVRTC program, compiled when a kernel of the
+// group is first needed: 0 the fit itself (LM, cost, model evaluation, GMW81
+// solve), 1 the searches, 2 the refill schedule and the warm-start fallback.
+constexpr int kGroups = 3;
+int group_of(int slot) {
+  switch (slot) {
+    case K_SEARCH_C1: case K_SEARCH_C0: case K_RS_C1_B1: case K_RS_C1_B0: case K_RS_C0_B1: case K_RS_C0_B0:
+      return 1;
+    case K_LMQ_C1_B1: case K_LMQ_C1_B0: case K_LMQ_C0_B1: case K_LMQ_C0_B0: case K_CHECK_C1: case K_CHECK_C0:
+    case K_SELECT_C1: case K_SELECT_C0: case K_LMC_C1_B1: case K_LMC_C1_B0: case K_LMC_C0_B1: case K_LMC_C0_B0:
+    case K_LMS_C1_B1: case K_LMS_C1_B0: case K_LMS_C0_B1: case K_LMS_C0_B0:
+      return 2;
+    default:
+      return 0;
+  }
+}
+
 std::string program_source(const char* model_source, const char* model_struct, int P, int C, int M, int dtype,
-                           int sdtype) {
+                           int sdtype, int group) {
   const char* ta = dtype == PCGB_DTYPE_F64 ? "double" : "float";
   const char* ts = sdtype == PCGB_DTYPE_F64 ? "double" : "float";
   std::ostringstream s;
-  s << "// pcgb fitter program: P=" << P << " C=" << C << " M=" << M << " state=" << ta << " solve=" << ts << "\n";
+  s << "// pcgb fitter program: P=" << P << " C=" << C << " M=" << M << " state=" << ta << " solve=" << ts
+    << " group=" << group << "\n";
   s << pcgb_embedded_lm_params_h << "\n" << pcgb_embedded_lm_kernel_cuh << "\n" << model_source << "\n";
   s << "typedef " << model_struct << " PcgbModel;\n";
   s << "static_assert(PcgbModel::P == " << P << " && PcgbModel::C == " << C << ", \"model shape\");\n";
   const char* bounds = "__launch_bounds__(256)";
-  for (int c = 1; c >= 0; --c)
+  const bool g0 = group == 0, g1 = group == 1, g2 = group == 2;
+  for (int c = 1; c >= 0 && g0; --c)
     for (int b = 1; b >= 0; --b)
       s << "extern \"C\" __global__ void " << bounds << " pcgb_lm_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
-  for (int c = 1; c >= 0; --c)
+  for (int c = 1; c >= 0 && g0; --c)
     s << "extern \"C\" __global__ void " << bounds << " pcgb_cost_c" << c
       << "(const PcgbLmParams a) { pcgb::cost_grid<PcgbModel, " << M << ", " << ta << ", " << (c ? "true" : "false")
       << ">(a); }\n";
-  s << "extern \"C\" __global__ void " << bounds << " pcgb_gmw81(const PcgbLmParams a) { pcgb::gmw81_grid<" << P
-    << ", " << ts << ">(a); }\n";
-  for (int c = 1; c >= 0; --c)
+  if (g0)
+    s << "extern \"C\" __global__ void " << bounds << " pcgb_gmw81(const PcgbLmParams a) { pcgb::gmw81_grid<" << P
+      << ", " << ts << ">(a); }\n";
+  for (int c = 1; c >= 0 && g2; --c)
     for (int b = 1; b >= 0; --b)
       s << "extern \"C\" __global__ void " << bounds << " pcgb_lmq_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_refill_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
-  for (int c = 1; c >= 0; --c)
+  for (int c = 1; c >= 0 && g2; --c)
+    for (int b = 1; b >= 0; --b) {
+      s << "extern \"C\" __global__ void " << bounds << " pcgb_lmc_c" << c << "_b" << b
+        << "(const PcgbLmParams a) { pcgb::lm_check_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
+        << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
+      s << "extern \"C\" __global__ void " << bounds << " pcgb_lms_c" << c << "_b" << b
+        << "(const PcgbLmParams a) { pcgb::lm_select_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
+        << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
+    }
+  for (int c = 1; c >= 0 && g1; --c)
     s << "extern \"C\" __global__ void " << bounds << " pcgb_search_c" << c
       << "(const PcgbLmParams a) { pcgb::search_step_grid<PcgbModel, " << M << ", " << ta << ", "
       << (c ? "true" : "false") << ">(a); }\n";
-  for (int c = 1; c >= 0; --c)
+  for (int c = 1; c >= 0 && g1; --c)
     for (int b = 1; b >= 0; --b)
       s << "extern \"C\" __global__ void " << bounds << " pcgb_rs_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::random_search_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
-  for (int c = 1; c >= 0; --c) {
+  for (int c = 1; c >= 0 && g2; --c) {
     s << "extern \"C\" __global__ void " << bounds << " pcgb_check_c" << c
       << "(const PcgbLmParams a) { pcgb::warm_check_grid<PcgbModel, " << M << ", " << ta << ", "
       << (c ? "true" : "false") << ">(a); }\n";
@@ -123,7 +157,7 @@ std::string program_source(const char* model_source, const char* model_struct, i
       << "(const PcgbLmParams a) { pcgb::warm_select_grid<PcgbModel, " << M << ", " << ta << ", "
       << (c ? "true" : "false") << ">(a); }\n";
   }
-  for (int c = 1; c >= 0; --c)
+  for (int c = 1; c >= 0 && g0; --c)
     s << "extern \"C\" __global__ void " << bounds << " pcgb_eval_c" << c
       << "(const PcgbLmParams a) { pcgb::eval_grid<PcgbModel, " << M << ", " << ta << ", " << (c ? "true" : "false")
       << ">(a); }\n";
@@ -201,14 +235,17 @@ int grid_for(int64_t n, int block) {
   return int(g);
 }
 
+int kernel_of(pcgb_fitter* ft, int slot, cudaKernel_t* out);
+
 int launch(pcgb_fitter* ft, KernelSlot slot, PcgbLmParams prm, int64_t n, int block, void* stream) {
-  if (!ft->k[slot]) return fail(PCGB_EINVAL, "kernel %s missing from program", kKernelNames[slot]);
+  cudaKernel_t kern = nullptr;
+  if (int rc = kernel_of(ft, slot, &kern)) return rc;
   if (block <= 0) block = kDefaultBlock;
   if (block > kMaxBlock || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to %d", kMaxBlock);
   if (n == 0) return PCGB_OK;
   if (!prm.vox_idx) prm.n_items = n;
   void* args[] = {&prm};
-  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(ft->k[slot]), dim3(grid_for(n, block)),
+  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(kern), dim3(grid_for(n, block)),
                                    dim3(block), args, 0, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, kKernelNames[slot]);
   return PCGB_OK;
@@ -272,9 +309,47 @@ int cubin_for_source(const std::string& src, const std::vector<std::string>& ext
 }
 
 int get_cubin(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata, int dtype,
-              int solve_dtype, const char* cache_dir, std::vector<char>& cubin, std::string& log) {
-  return cubin_for_source(program_source(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype), {},
-                          cache_dir, cubin, log);
+              int solve_dtype, const char* cache_dir, int group, std::vector<char>& cubin, std::string& log) {
+  return cubin_for_source(
+      program_source(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, group), {}, cache_dir,
+      cubin, log);
+}
+
+// Compile (or read from the cache) and load kernel group g of a fitter.
+int load_group(pcgb_fitter* ft, int g) {
+  std::vector<char> cubin;
+  std::string log;
+  if (int rc = get_cubin(ft->source.c_str(), ft->structname.c_str(), ft->P, ft->C, ft->M, ft->dtype, ft->sdtype,
+                         ft->cache_dir.empty() ? nullptr : ft->cache_dir.c_str(), g, cubin, log))
+    return rc;
+  cudaLibrary_t lib = nullptr;
+  cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaLibraryLoadData");
+  cudaKernel_t ks[K_COUNT] = {};
+  for (int i = 0; i < K_COUNT; ++i) {
+    if (group_of(i) != g) continue;
+    e = cudaLibraryGetKernel(&ks[i], lib, kKernelNames[i]);
+    if (e != cudaSuccess) {
+      cudaLibraryUnload(lib);
+      return cuda_fail(e, kKernelNames[i]);
+    }
+  }
+  for (int i = 0; i < K_COUNT; ++i)
+    if (group_of(i) == g) ft->k[i] = ks[i];
+  ft->lib[g] = lib;
+  if (!log.empty()) ft->log += log;
+  return PCGB_OK;
+}
+
+// The kernel of a slot, its group compiled and loaded on first use.
+int kernel_of(pcgb_fitter* ft, int slot, cudaKernel_t* out) {
+  std::lock_guard<std::mutex> lock(ft->mu);
+  if (!ft->k[slot]) {
+    if (int rc = load_group(ft, group_of(slot))) return rc;
+  }
+  if (!ft->k[slot]) return fail(PCGB_EINVAL, "kernel %s missing from program", kKernelNames[slot]);
+  *out = ft->k[slot];
+  return PCGB_OK;
 }
 
 static_assert(sizeof(PcgbMultiParams) <= 32000, "multi-model launch parameters exceed the 32 KB kernel parameter limit");
@@ -331,12 +406,17 @@ int pcgb_fitter_compile(const char* model_source, const char* model_struct, int 
                         int dtype, int solve_dtype, const char* cache_dir, char* log_buf, size_t log_len) {
   g_err.clear();
   if (int rc = validate_create(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype)) return rc;
-  std::vector<char> cubin;
-  std::string log;
-  if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, cubin, log))
-    return rc;
+  std::string all;
+  for (int g = 0; g < kGroups; ++g) {
+    std::vector<char> cubin;
+    std::string log;
+    if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, g, cubin,
+                           log))
+      return rc;
+    all += log;
+  }
   if (log_buf && log_len) {
-    std::snprintf(log_buf, log_len, "%s", log.c_str());
+    std::snprintf(log_buf, log_len, "%s", all.c_str());
   }
   return PCGB_OK;
 }
@@ -347,11 +427,6 @@ int pcgb_fitter_create(const char* model_source, const char* model_struct, int n
   if (!out) return fail(PCGB_EINVAL, "out is NULL");
   *out = nullptr;
   if (int rc = validate_create(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype)) return rc;
-  std::vector<char> cubin;
-  std::string log;
-  if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, cubin, log))
-    return rc;
-
   auto* ft = new (std::nothrow) pcgb_fitter();
   if (!ft) return fail(PCGB_ENOMEM, "out of host memory");
   ft->P = nparam;
@@ -359,24 +434,19 @@ int pcgb_fitter_create(const char* model_source, const char* model_struct, int n
   ft->M = ndata;
   ft->dtype = dtype;
   ft->sdtype = solve_dtype;
-  ft->log = log;
+  ft->source = model_source;
+  ft->structname = model_struct;
+  ft->cache_dir = cache_dir ? cache_dir : "";
   cudaError_t e = cudaGetDevice(&ft->device);
   if (e != cudaSuccess) {
     delete ft;
     return cuda_fail(e, "cudaGetDevice");
   }
-  e = cudaLibraryLoadData(&ft->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
-  if (e != cudaSuccess) {
+  // the fit kernels now (a model that does not compile fails here); the
+  // searches and the refill / fallback kernels when first used
+  if (int rc = load_group(ft, 0)) {
     delete ft;
-    return cuda_fail(e, "cudaLibraryLoadData");
-  }
-  for (int i = 0; i < K_COUNT; ++i) {
-    e = cudaLibraryGetKernel(&ft->k[i], ft->lib, kKernelNames[i]);
-    if (e != cudaSuccess) {
-      cudaLibraryUnload(ft->lib);
-      delete ft;
-      return cuda_fail(e, kKernelNames[i]);
-    }
+    return rc;
   }
   *out = ft;
   return PCGB_OK;
@@ -525,8 +595,9 @@ int pcgb_multi_run(pcgb_multi* m, const pcgb_multi_job* jobs, int n_jobs, const 
 int pcgb_fitter_destroy(pcgb_fitter* ft) {
   if (!ft) return PCGB_OK;
   int rc = PCGB_OK;
-  if (ft->lib) {
-    cudaError_t e = cudaLibraryUnload(ft->lib);
+  for (int g = 0; g < kGroups; ++g) {
+    if (!ft->lib[g]) continue;
+    cudaError_t e = cudaLibraryUnload(ft->lib[g]);
     if (e != cudaSuccess) rc = cuda_fail(e, "cudaLibraryUnload");
   }
   delete ft;
@@ -535,13 +606,28 @@ int pcgb_fitter_destroy(pcgb_fitter* ft) {
 
 const char* pcgb_fitter_log(const pcgb_fitter* ft) { return ft ? ft->log.c_str() : ""; }
 
+// Fallback epilogue of an LM launch: 1 = the warm fit's check (pcgb_lm_run_check),
+// 2 = the refit's select (pcgb_lm_run_select).
+struct FallbackArgs {
+  int mode = 0;
+  const double* init_values = nullptr;
+  double lam0 = 5.0;
+  void* cost = nullptr;
+  void* pars_backup = nullptr;
+  void* cost_backup = nullptr;
+  int32_t* fb_idx = nullptr;
+  uint32_t* fb_count = nullptr;
+  int8_t* which = nullptr;
+};
+
 static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
                        const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
                        double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
                        void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
                        const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
                        int block, const int32_t* vox_idx, int64_t n_items, void* stream,
-                       uint32_t* work_counter = nullptr, int grid = 0, const uint32_t* n_items_dev = nullptr) {
+                       uint32_t* work_counter = nullptr, int grid = 0, const uint32_t* n_items_dev = nullptr,
+                       const FallbackArgs* fb = nullptr) {
   g_err.clear();
   if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
   if (nprobs < 0 || iters < 0) return fail(PCGB_EINVAL, "nprobs and iters must be >= 0");
@@ -585,6 +671,29 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
   prm.dec = dec;
   const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_LM_C1_B1 : K_LM_C1_B0)
                                              : (bounds_stride == 0 ? K_LM_C0_B1 : K_LM_C0_B0);
+  if (fb) {
+    if (nprobs > (int64_t(1) << 31) - 1) return fail(PCGB_ERANGE, "the fallback indexes voxels with int32");
+    if (!fb->fb_count || !fb->fb_idx || !fb->cost || !fb->pars_backup || !fb->cost_backup)
+      return fail(PCGB_EINVAL, "fallback buffers (cost, backups, fb_idx, fb_count) are required");
+    prm.cost = fb->cost;
+    prm.pars_backup = fb->pars_backup;
+    prm.cost_backup = fb->cost_backup;
+    prm.fb_idx = fb->fb_idx;
+    prm.fb_count = fb->fb_count;
+    prm.which = reinterpret_cast<signed char*>(fb->which);
+    if (fb->mode == 1) {
+      if (!fb->init_values) return fail(PCGB_EINVAL, "init_values are required");
+      for (int k = 0; k < ft->P; ++k) prm.init_val[k] = float(fb->init_values[k]);
+      prm.lam0 = fb->lam0;
+      cudaError_t e = cudaMemsetAsync(fb->fb_count, 0, 2 * sizeof(uint32_t), static_cast<cudaStream_t>(stream));
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+      return launch(ft, KernelSlot(slot + (K_LMC_C1_B1 - K_LM_C1_B1)), prm, nprobs, block, stream);
+    }
+    prm.vox_idx = fb->fb_idx;
+    prm.n_items = nprobs;
+    prm.n_items_dev = fb->fb_count;
+    return launch(ft, KernelSlot(slot + (K_LMS_C1_B1 - K_LM_C1_B1)), prm, nprobs, block, stream);
+  }
   if (work_counter) {
     // refill schedule: persistent grid, warps claim 256-item chunks from the counter
     const KernelSlot q = KernelSlot(slot + (K_LMQ_C1_B1 - K_LM_C1_B1));
@@ -601,6 +710,8 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
     prm.n_items_dev = n_items_dev;
     if (block <= 0) block = kDefaultBlock;
     if (block > kMaxBlock || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to %d", kMaxBlock);
+    cudaKernel_t kq = nullptr;
+    if (int rc = kernel_of(ft, q, &kq)) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
@@ -608,14 +719,14 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
       int per_sm = 0, dev = 0, sms = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(ft->k[q]), block, 0);
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(kq), block, 0);
       if (e != cudaSuccess || per_sm < 1) per_sm = 1;
       grid = per_sm * sms;
       const int64_t need = (prm.n_items + block - 1) / block;
       if (grid > need) grid = int(need);
     }
     void* args[] = {&prm};
-    e = cudaLaunchKernel(reinterpret_cast<const void*>(ft->k[q]), dim3(grid), dim3(block), args, 0, st);
+    e = cudaLaunchKernel(reinterpret_cast<const void*>(kq), dim3(grid), dim3(block), args, 0, st);
     if (e != cudaSuccess) return cuda_fail(e, kKernelNames[q]);
     return PCGB_OK;
   }
@@ -653,6 +764,49 @@ int pcgb_lm_run_refill(pcgb_fitter* ft, const void* consts, int64_t consts_strid
   return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
                      params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
                      protocol_len, lb_host, ub_host, block, vox_idx, n_items, stream, work_counter, grid, n_items_dev);
+}
+
+int pcgb_lm_run_check(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                      const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                      double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                      void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                      const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                      int block, const double* init_values, double lam0, void* cost, void* pars_backup,
+                      void* cost_backup, int32_t* fb_idx, uint32_t* fb_count, void* stream) {
+  g_err.clear();
+  FallbackArgs fb;
+  fb.mode = 1;
+  fb.init_values = init_values;
+  fb.lam0 = lam0;
+  fb.cost = cost;
+  fb.pars_backup = pars_backup;
+  fb.cost_backup = cost_backup;
+  fb.fb_idx = fb_idx;
+  fb.fb_count = fb_count;
+  return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
+                     params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
+                     protocol_len, lb_host, ub_host, block, nullptr, 0, stream, nullptr, 0, nullptr, &fb);
+}
+
+int pcgb_lm_run_select(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, void* params, void* step, void* lam, int8_t* step_type,
+                       void* f, void* first_f, void* last_f, int32_t* iters_done, int64_t nprobs, int iters,
+                       const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                       int block, void* cost, const void* pars_backup, const void* cost_backup,
+                       const int32_t* fb_idx, uint32_t* fb_count, int8_t* which, void* stream) {
+  g_err.clear();
+  FallbackArgs fb;
+  fb.mode = 2;
+  fb.cost = cost;
+  fb.pars_backup = const_cast<void*>(pars_backup);
+  fb.cost_backup = const_cast<void*>(cost_backup);
+  fb.fb_idx = const_cast<int32_t*>(fb_idx);
+  fb.fb_count = fb_count;
+  fb.which = which;
+  return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
+                     params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
+                     protocol_len, lb_host, ub_host, block, nullptr, 0, stream, nullptr, 0, nullptr, &fb);
 }
 
 int pcgb_warm_check(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
@@ -736,7 +890,8 @@ int pcgb_warm_select(pcgb_fitter* ft, const void* consts, int64_t consts_stride,
   prm.which = reinterpret_cast<signed char*>(which);
   prm.N = nprobs;
   const KernelSlot slot = consts_stride == 0 ? K_SELECT_C1 : K_SELECT_C0;
-  if (!ft->k[slot]) return fail(PCGB_EINVAL, "kernel %s missing from program", kKernelNames[slot]);
+  cudaKernel_t ksel = nullptr;
+  if (int rc = kernel_of(ft, slot, &ksel)) return rc;
   // the flagged count is known only on the device: a grid of 8 blocks per SM strides over it
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
@@ -745,7 +900,7 @@ int pcgb_warm_select(pcgb_fitter* ft, const void* consts, int64_t consts_stride,
   const int64_t need = (nprobs + 255) / 256;
   if (grid > need) grid = int(need);
   void* args[] = {&prm};
-  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(ft->k[slot]), dim3(grid), dim3(256), args, 0,
+  cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(ksel), dim3(grid), dim3(256), args, 0,
                                    static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, kKernelNames[slot]);
   return PCGB_OK;

@@ -342,6 +342,36 @@ class SecondOrderLevenbergMarquardt:
             _lib.check("pcgb_lm_run", rc)
         return None
 
+    def _lm_args(self, iters, tol, mu, eta, acc, dec, block):
+        """The arguments every LM entry point starts with (pcgb_lm_run's, up to block)."""
+        pv, plen = self._proto_args()
+        lbh = (ctypes.c_double * self.nparam)(*(self._lb_host or [0.0] * self.nparam))
+        ubh = (ctypes.c_double * self.nparam)(*(self._ub_host or [0.0] * self.nparam))
+        return (self.build().handle, _ptr(self.consts_t), self._cstride, _ptr(self.data_t), _ptr(self.lower_bound_t),
+                _ptr(self.upper_bound_t), self._bstride, float(tol), float(mu), float(eta), float(acc), float(dec),
+                _ptr(self.pars_t), _ptr(self.step_t), _ptr(self.lam_t), _ptr(self.step_type_t), _ptr(self.f_t),
+                _ptr(self.first_f), _ptr(self.last_f), _ptr(self.iters_t), self.Nprobs, int(iters), pv, plen,
+                lbh if self._bstride == 0 else None, ubh if self._bstride == 0 else None, int(block))
+
+    def run_check(self, iters: int, init_values, lam_refit: float, cost, pars_backup, cost_backup, fb_idx, fb_count,
+                  tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0, block: int = 0):
+        """run() with the warm-start fallback check as its epilogue (pcgb_lm_run_check)."""
+        with torch.cuda.device(self.pars_t.device):
+            iv = (ctypes.c_double * self.nparam)(*[float(x) for x in init_values])
+            rc = _lib.lib().pcgb_lm_run_check(*self._lm_args(iters, tol, mu, eta, acc, dec, block), iv,
+                                               float(lam_refit), _ptr(cost), _ptr(pars_backup), _ptr(cost_backup),
+                                               _ptr(fb_idx), _ptr(fb_count), ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_lm_run_check", rc)
+
+    def run_select(self, iters: int, cost, pars_backup, cost_backup, fb_idx, fb_count, which=None, tol=1e-8,
+                   mu=0.25, eta=0.75, acc=0.2, dec=2.0, block: int = 0):
+        """Refit of the flagged voxels with the select as its epilogue (pcgb_lm_run_select)."""
+        with torch.cuda.device(self.pars_t.device):
+            rc = _lib.lib().pcgb_lm_run_select(*self._lm_args(iters, tol, mu, eta, acc, dec, block), _ptr(cost),
+                                                _ptr(pars_backup), _ptr(cost_backup), _ptr(fb_idx), _ptr(fb_count),
+                                                _ptr(which), ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_lm_run_select", rc)
+
     def _run_refill(self, iters, tol, mu, eta, acc, dec, block, vox_idx, n_items, grid: int = 0, n_items_dev=None):
         with torch.cuda.device(self.pars_t.device):
             prog = self.build()

@@ -178,14 +178,16 @@ class WarmStartFitter:
         return self._buf
 
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
-            lam0: float = 1e-3, timings: dict | None = None, fused: bool = True, events: list | None = None):
+            lam0: float = 1e-3, timings: dict | None = None, fused="epilogue", events: list | None = None):
         """Warm-started fit of data (M, N); returns a WarmFit.
 
-        ``fused`` (default) runs steps 3-5 as three kernels that never return
-        the flagged count to the host (check + compaction + state reset in one
-        pass; the refit takes the count from device memory; cost + select in
-        one pass); ``fused=False`` runs them as the separate pipeline kernels
+        ``fused="epilogue"`` (default) runs the fallback check as the epilogue
+        of the warm LM launch and the select as the epilogue of the refit
+        launch (the flagged count never returns to the host, the signals are
+        read once); ``fused=True`` runs check, refit and select as three
+        kernels of their own; ``fused=False`` as the separate pipeline kernels
         (cost, constant start, cost, flags, prepare, refit, cost, select).
+        All three give the same results.
         ``timings`` (a dict) receives per-stage milliseconds (synchronises);
         ``events`` (a list) receives (stage, CUDA event) pairs recorded after
         each stage on the current stream, without synchronising.
@@ -212,6 +214,21 @@ class WarmStartFitter:
         solm.setup(pars, prot, data, lb, ub)
         solm.lam_t.fill_(lam0)
         mark("setup")
+        if fused == "epilogue":
+            # the check as the warm LM's epilogue, the select as the refit's
+            b = self._buffers(P, N, dev)
+            solm.run_check(iters_warm, w.init_values, 5.0, b["cost"], b["backup"], b["cost_b"], b["idx"],
+                           b["counts"])
+            mark("lm_warm")
+            mark("check")
+            solm.run_select(iters_fallback, b["cost"], b["backup"], b["cost_b"], b["idx"], b["counts"])
+            mark("refit")
+            mark("select")
+            if timings is not None:
+                torch.cuda.synchronize()
+                for (n0, e0), (n1, e1) in zip(ev[:-1], ev[1:]):
+                    timings[n1] = timings.get(n1, 0.0) + e0.elapsed_time(e1)
+            return WarmFit(pars, b["cost"], b["counts"], solm.step_type_t)
         solm.run(iters_warm)
         mark("lm_warm")
         if fused:

@@ -96,8 +96,10 @@ def test_fused_inference_matches_oracle(log_in, impl):
 
 @pytest.mark.parametrize("n", [1, 127, 129, 1000, 65537])
 def test_tcgen05_inference_matches_mma(n):
-    """Both inference kernels round to bf16 at the same points; only the fp32
-    summation order inside the tensor cores differs."""
+    """Both inference kernels round to bf16 at the same points; the tcgen05
+    kernel adds each bias as two bf16 terms inside the MMA (b to 2^-16), so
+    pre-activations differ in the last fp32 bits and an occasional bf16
+    rounding of an activation flips."""
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     true, data, *_ = w.generate(max(n, 2), seed=9)
     data, true = data[:, :n], true[:, :n]
@@ -109,8 +111,8 @@ def test_tcgen05_inference_matches_mma(n):
     torch.cuda.synchronize()
     assert net.tc_status() == 0
     np.testing.assert_allclose(b.cpu().numpy(), a.cpu().numpy(), rtol=1e-2, atol=1e-7)
-    # most outputs are bitwise equal: a differing fp32 sum only matters where it changes a bf16 rounding
-    assert float((a == b).float().mean()) > 0.5
+    rel = ((a - b).abs() / a.abs().clamp_min(1e-30)).flatten()
+    assert float(rel.median()) < 1e-3
 
 
 def test_training_reduces_loss_and_graph_matches_eager():

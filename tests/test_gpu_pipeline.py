@@ -83,15 +83,18 @@ def test_fallback_refits_flagged_voxels():
     assert np.all(cost[refit] <= c_plain.cpu().numpy()[refit] * (1 + 1e-6) + 1e-3)
 
 
-@pytest.mark.parametrize("per_voxel_bounds,schedule", [(False, "grid"), (True, "grid"), (False, "refill")])
-def test_fused_fallback_matches_separate_kernels(per_voxel_bounds, schedule):
-    """Check + refit + select as three fused kernels (no host read of the
-    flagged count) give the same fits, costs and counts as the separate
+@pytest.mark.parametrize("per_voxel_bounds,schedule,mode", [(False, "grid", True), (True, "grid", True),
+                                                            (False, "refill", True), (False, "grid", "epilogue"),
+                                                            (True, "grid", "epilogue")])
+def test_fused_fallback_matches_separate_kernels(per_voxel_bounds, schedule, mode):
+    """Check + refit + select as three fused kernels, or as the epilogues of
+    the warm LM and the refit launches (no host read of the flagged count
+    either way), give the same fits, costs and counts as the separate
     pipeline kernels."""
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     _, data = pipeline.synth_gpu(w, 50001, seed=7, device=DEV)
     out = []
-    for fused in (False, True):
+    for fused in (False, mode):
         wf = pipeline.WarmStartFitter(w, _BadNet(w))
         wf.refit_schedule = schedule
         if per_voxel_bounds:
