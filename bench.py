@@ -42,7 +42,9 @@ Reported (one JSON line from rank 0):
 `--impl reference` runs the reference arm: the reference algorithm on the host
 cores (its own generated kernel built for the host when available, else the
 CPU oracle in the reference's fp32 arithmetic) at its 1e-4 budget, one bounded
-sample per step.
+sample per step; where its generated kernel was also built for the GPU, the
+line adds that kernel's fits/s on this GPU, launched as the reference's run()
+does (`gpu_reference_kernel`, informational).
 """
 from __future__ import annotations
 
@@ -585,6 +587,42 @@ def _config(args, ws, k_warm=None, k_plain=None):
             "l2": "inputs larger than L2 (1.07 GB signals per GPU)", "parallelism": f"voxel shards x{ws}"}
 
 
+def reference_gpu_kernel(steps: int = 3):
+    """The reference's own LM kernel on this GPU, launched as its run() does
+    (oracle/_ref cubin built from the reference tree; 32-thread blocks, one
+    launch per iteration): IVIM-10 8,388,608 voxels x 100 iterations, and
+    IVIM-16 16,777,216 voxels at the plain LM's 1e-4 budget (8 iterations)."""
+    import torch
+    from oracle import ref_gpu
+    from pycompute_gb300 import pipeline, synth
+
+    out = {"kernel": "reference generated LM kernel (printf dropped, parameter loads bounded), sm_103a",
+           "launch": "ceil(N/32) blocks x 32 threads, one launch per iteration, protocol tiled per voxel"}
+    for name, w, n, iters in (("ivim10_8.4M_100it", synth.ivim(), 256 * 256 * 128, 100),
+                              ("ivim16_16.7M_8it_at_1e-4", synth.ivim(synth.ivim_b16(), name="ivim16"), 1 << 24, 8)):
+        if not ref_gpu.available(w.M):
+            out[name] = {"unavailable": f"oracle/_ref cubin for {w.M} samples not built"}
+            continue
+        _, data = pipeline.synth_gpu(w, n, seed=1000, device="cuda")
+        init = pipeline.init_constant(data, w.init_values)
+        consts = torch.tensor(w.protocol, device="cuda")[:, None].expand(w.M, n).contiguous()
+        lb = torch.tensor(w.lb, device="cuda")[:, None].expand(4, n).contiguous()
+        ub = torch.tensor(w.ub, device="cuda")[:, None].expand(4, n).contiguous()
+        ref = ref_gpu.RefGpuIVIM(w.M)
+        pars = init.clone()
+
+        def step():
+            pars.copy_(init)
+            ref.setup(pars, consts, data, lb, ub)
+            ref.run(iters)
+
+        ms = _time_ms(step, warmup=1, reps=steps)
+        out[name] = {"voxels": n, "iters": iters, "fits_per_s": n / (ms / 1e3), "ms_per_fit": ms}
+        del ref, pars, consts, lb, ub, data, init
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_reference_arm(args):
     ws, rank, local = _dist()
     if rank != 0:
@@ -595,6 +633,14 @@ def run_reference_arm(args):
         if s >= args.warmup:
             vals.append(last["value"])
     value = statistics.median(vals)
+    gpu = None
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            gpu = reference_gpu_kernel()
+    except Exception as e:  # informational only: the reference arm's value is the CPU measurement
+        gpu = {"unavailable": f"{type(e).__name__}: {e}"}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
@@ -603,6 +649,7 @@ def run_reference_arm(args):
         "cpu_baseline": {"value": value, "unit": "fits/s", "cores": last["cores"], "kind": last["kind"],
                          "sample": last["sample"]},
         "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_reference_kernel": gpu,
     }
     print(json.dumps(line), flush=True)
     return 0
