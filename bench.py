@@ -37,7 +37,11 @@ Reported (one JSON line from rank 0):
                 its own 1e-4 budget on a bounded IVIM-16 sample
   plain_lm_ivim10_8.4M  the plain LM at scale (IVIM-10, 8,388,608 voxels,
                 100 iterations) with its accuracy against the FP64 fitter
-  mixed_batch   four models in one persistent launch vs one launch per model
+  mixed_batch   four models in one persistent launch vs one launch per model,
+                with each model's accuracy against the all-FP64 fitter
+  precision_stress  ill-conditioned IVIM-10 (SNR 10-20, small f): per-parameter
+                error quantiles of the FP64-solve and fp32-solve fitters
+                against the all-FP64 fitter
 
 `--impl reference` runs the reference arm: the reference algorithm on the host
 cores (its own generated kernel built for the host when available, else the
@@ -571,12 +575,66 @@ def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
     ms_graph = _time_ms(run_graph)
     ms_single = _time_ms(run_singles)
     its = [float(j.iters.double().mean()) for j in jobs]
+    # accuracy of the one-launch results against the all-FP64 fitter (same LM,
+    # same start, same iterations), per model
+    run_multi()
+    torch.cuda.synchronize()
+    acc = {}
+    for w, j, i0 in zip(ws, jobs, inits):
+        s64 = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float64)
+        p64 = i0.double()
+        s64.setup(p64, list(w.protocol), j.data.double(), list(w.lb), list(w.ub))
+        s64.run(iters)
+        med, frac = _median_rel_gpu(j.pars, p64)
+        acc[w.name] = {"median_rel_err": med, "frac_voxels_gt_1e-4": frac,
+                       "per_param_median": _per_param_median(j.pars, p64)}
+        del s64, p64
     return {"workload": "mixed_vfa8_t2s16_ivim10_biexp32", "voxels": total, "iters": iters,
             "autotuned": {k: tuned.get(k) for k in ("block", "maxrreg", "chunk", "order", "ms")},
             "tune_s": round(tune_s, 1),
             "one_launch_fits_per_s": total / (ms_multi / 1e3), "graph_fits_per_s": total / (ms_graph / 1e3),
             "per_model_launches_fits_per_s": total / (ms_single / 1e3), "mean_iters_per_model": its,
-            "ms": {"one_launch": ms_multi, "graph": ms_graph, "per_model": ms_single}}
+            "ms": {"one_launch": ms_multi, "graph": ms_graph, "per_model": ms_single},
+            "accuracy_vs_fp64_same_iters": acc}
+
+
+def precision_stress(n=1 << 21, iters=100, seed=400):
+    """Ill-conditioned IVIM-10 (SNR 10-20, f in [0.005, 0.05]): the FP32-bulk /
+    FP64-solve fitter and the fp32-solve fitter against the all-FP64 fitter
+    (same LM, same start, same iterations; and against its converged fit)."""
+    import torch
+    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, pipeline, synth
+
+    w = synth.ivim(snr=(10.0, 20.0), f_range=(0.005, 0.05), name="ivim10_stress")
+    _, data = pipeline.synth_gpu(w, n, seed=seed, device="cuda")
+    init = pipeline.init_constant(data, w.init_values)
+    prot, lb, ub = list(w.protocol), list(w.lb), list(w.ub)
+
+    def fit(dtype, solve, k, tol=1e-8):
+        solm = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, dtype, solve_dtype=solve)
+        p = init.to(dtype).clone()
+        solm.setup(p, prot, data.to(dtype), lb, ub)
+        solm.run(k, tol=tol)
+        torch.cuda.synchronize()
+        return p
+
+    p64_same = fit(torch.float64, torch.float64, iters)
+    p64_conv = fit(torch.float64, torch.float64, 300, tol=1e-30)
+
+    def report(p, ref):
+        r = ((p.double() - ref).abs() / ref.abs().clamp_min(1e-30))
+        r = torch.nan_to_num(r, nan=float("inf"))
+        q = torch.quantile(r.float(), torch.tensor([0.5, 0.9, 0.99], device=r.device), dim=1).T
+        worst = r.amax(dim=0)
+        return {"per_param_q50_q90_q99": [[float(x) for x in row] for row in q],
+                "median_rel_err": float(worst.median()), "frac_voxels_gt_1e-4": float((worst > 1e-4).double().mean())}
+
+    out = {"workload": "ivim10_stress_2M (SNR 10-20, f in [0.005, 0.05])", "voxels": n, "iters": iters,
+           "params": list(w.pars)}
+    for name, solve in (("f32_state_f64_solve", torch.float64), ("f32_state_f32_solve", torch.float32)):
+        p = fit(torch.float32, solve, iters)
+        out[name] = {"vs_fp64_same_iters": report(p, p64_same), "vs_fp64_converged": report(p, p64_conv)}
+    return out
 
 
 def _config(args, ws, k_warm=None, k_plain=None):
@@ -674,6 +732,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ivim10", action="store_true", help="skip the IVIM-10 plain-LM block")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-stress", action="store_true", help="skip the precision-stress block")
     ap.add_argument("--no-fp64-check", action="store_true", help="IVIM-10 block without its FP64 comparison")
     ap.add_argument("--only-ivim10", action="store_true", help="print only the IVIM-10 plain-LM block")
     ap.add_argument("--only-mixed", action="store_true", help="print only the mixed-model block")
@@ -709,6 +768,7 @@ def main():
     ivim10 = plain_ivim10_block(args, dev, fp64_check=not args.no_fp64_check) if single and not args.no_ivim10 \
         else None
     mixed = mixed_batch_comparison() if single and not args.no_mixed else None
+    stress = precision_stress() if single and not args.no_stress else None
     cpu = None
     if single and not args.no_cpu:
         cpu = cpu_reference_at_tol(target_s=args.cpu_seconds)
@@ -750,6 +810,7 @@ def main():
             "warm_start": h["detail"],
             "plain_lm_ivim10_8.4M": ivim10,
             "mixed_batch": mixed,
+            "precision_stress": stress,
             "cpu_baseline": cpu,
             "gpu_launches": 5 * args.steps,
             "clocks": h["clocks"],
