@@ -77,6 +77,7 @@ struct pcgb_fitter {
   int P = 0, C = 0, M = 0, dtype = 0, sdtype = 0;
   int device = -1;
   cudaLibrary_t lib[3] = {};  // one per kernel group, loaded on first use
+  int lm_min_blocks[3] = {};  // occupancy hint the group's LM kernels were built with (0: none)
   cudaKernel_t k[K_COUNT] = {};
   std::string source, structname, cache_dir;
   std::mutex mu;
@@ -102,8 +103,24 @@ int group_of(int slot) {
   }
 }
 
+// The LM kernels for a shared protocol and shared bounds (the common case,
+// the variant with the fewest registers) are first built for at least
+// kLmMinBlocks resident 128-thread blocks per SM (a register cap: more warps
+// to hide the FP64 pipe's latency); a model whose capped kernels would spill
+// more than kLmMaxSpillBytes per thread is rebuilt without the cap.
+bool is_lm_slot(int slot) {
+  return slot == K_LM_C1_B1 || slot == K_LMQ_C1_B1 || slot == K_LMC_C1_B1 || slot == K_LMS_C1_B1;
+}
+
+constexpr int kLmMinBlocks = 5;
+constexpr int kLmMaxThreads = 128;
+// A few spilled words per thread stay in L1 and cost less than the occupancy
+// gains (IVIM-16: 32 bytes, and the capped kernel is 5 % faster); more than
+// this and the cap is dropped.
+constexpr size_t kLmMaxSpillBytes = 64;
+
 std::string program_source(const char* model_source, const char* model_struct, int P, int C, int M, int dtype,
-                           int sdtype, int group) {
+                           int sdtype, int group, int lm_min_blocks) {
   const char* ta = dtype == PCGB_DTYPE_F64 ? "double" : "float";
   const char* ts = sdtype == PCGB_DTYPE_F64 ? "double" : "float";
   std::ostringstream s;
@@ -113,10 +130,13 @@ std::string program_source(const char* model_source, const char* model_struct, i
   s << "typedef " << model_struct << " PcgbModel;\n";
   s << "static_assert(PcgbModel::P == " << P << " && PcgbModel::C == " << C << ", \"model shape\");\n";
   const char* bounds = "__launch_bounds__(256)";
+  const std::string lmb = lm_min_blocks > 0 ? "__launch_bounds__(" + std::to_string(kLmMaxThreads) + ", " +
+                                                  std::to_string(lm_min_blocks) + ")"
+                                            : std::string(bounds);
   const bool g0 = group == 0, g1 = group == 1, g2 = group == 2;
   for (int c = 1; c >= 0 && g0; --c)
     for (int b = 1; b >= 0; --b)
-      s << "extern \"C\" __global__ void " << bounds << " pcgb_lm_c" << c << "_b" << b
+      s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lm_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
   for (int c = 1; c >= 0 && g0; --c)
@@ -128,15 +148,15 @@ std::string program_source(const char* model_source, const char* model_struct, i
       << ", " << ts << ">(a); }\n";
   for (int c = 1; c >= 0 && g2; --c)
     for (int b = 1; b >= 0; --b)
-      s << "extern \"C\" __global__ void " << bounds << " pcgb_lmq_c" << c << "_b" << b
+      s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lmq_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_refill_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
   for (int c = 1; c >= 0 && g2; --c)
     for (int b = 1; b >= 0; --b) {
-      s << "extern \"C\" __global__ void " << bounds << " pcgb_lmc_c" << c << "_b" << b
+      s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lmc_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_check_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
-      s << "extern \"C\" __global__ void " << bounds << " pcgb_lms_c" << c << "_b" << b
+      s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lms_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_select_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
     }
@@ -236,11 +256,12 @@ int grid_for(int64_t n, int block) {
 }
 
 int kernel_of(pcgb_fitter* ft, int slot, cudaKernel_t* out);
+int lm_block(const pcgb_fitter* ft, int slot, int block);
 
 int launch(pcgb_fitter* ft, KernelSlot slot, PcgbLmParams prm, int64_t n, int block, void* stream) {
   cudaKernel_t kern = nullptr;
   if (int rc = kernel_of(ft, slot, &kern)) return rc;
-  if (block <= 0) block = kDefaultBlock;
+  block = lm_block(ft, slot, block);
   if (block > kMaxBlock || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to %d", kMaxBlock);
   if (n == 0) return PCGB_OK;
   if (!prm.vox_idx) prm.n_items = n;
@@ -309,36 +330,67 @@ int cubin_for_source(const std::string& src, const std::vector<std::string>& ext
 }
 
 int get_cubin(const char* model_source, const char* model_struct, int nparam, int nconst, int ndata, int dtype,
-              int solve_dtype, const char* cache_dir, int group, std::vector<char>& cubin, std::string& log) {
+              int solve_dtype, const char* cache_dir, int group, int lm_min_blocks, std::vector<char>& cubin,
+              std::string& log) {
   return cubin_for_source(
-      program_source(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, group), {}, cache_dir,
-      cubin, log);
+      program_source(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, group, lm_min_blocks),
+      {}, cache_dir, cubin, log);
 }
 
-// Compile (or read from the cache) and load kernel group g of a fitter.
+// Compile (or read from the cache) and load kernel group g of a fitter: first
+// with the LM kernels' occupancy hint, again without it if any of them spills
+// (local memory in use).
 int load_group(pcgb_fitter* ft, int g) {
-  std::vector<char> cubin;
-  std::string log;
-  if (int rc = get_cubin(ft->source.c_str(), ft->structname.c_str(), ft->P, ft->C, ft->M, ft->dtype, ft->sdtype,
-                         ft->cache_dir.empty() ? nullptr : ft->cache_dir.c_str(), g, cubin, log))
-    return rc;
-  cudaLibrary_t lib = nullptr;
-  cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaLibraryLoadData");
-  cudaKernel_t ks[K_COUNT] = {};
-  for (int i = 0; i < K_COUNT; ++i) {
-    if (group_of(i) != g) continue;
-    e = cudaLibraryGetKernel(&ks[i], lib, kKernelNames[i]);
-    if (e != cudaSuccess) {
-      cudaLibraryUnload(lib);
-      return cuda_fail(e, kKernelNames[i]);
+  const int tries[2] = {g == 1 ? 0 : kLmMinBlocks, 0};
+  for (int t = 0; t < 2; ++t) {
+    if (t == 1 && tries[0] == 0) break;
+    std::vector<char> cubin;
+    std::string log;
+    if (int rc = get_cubin(ft->source.c_str(), ft->structname.c_str(), ft->P, ft->C, ft->M, ft->dtype, ft->sdtype,
+                           ft->cache_dir.empty() ? nullptr : ft->cache_dir.c_str(), g, tries[t], cubin, log))
+      return rc;
+    cudaLibrary_t lib = nullptr;
+    cudaError_t e = cudaLibraryLoadData(&lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaLibraryLoadData");
+    cudaKernel_t ks[K_COUNT] = {};
+    bool spills = false;
+    for (int i = 0; i < K_COUNT; ++i) {
+      if (group_of(i) != g) continue;
+      e = cudaLibraryGetKernel(&ks[i], lib, kKernelNames[i]);
+      if (e != cudaSuccess) {
+        cudaLibraryUnload(lib);
+        return cuda_fail(e, kKernelNames[i]);
+      }
+      if (tries[t] > 0 && is_lm_slot(i)) {
+        cudaFuncAttributes fa{};
+        e = cudaFuncGetAttributes(&fa, reinterpret_cast<const void*>(ks[i]));
+        if (e != cudaSuccess) {
+          cudaLibraryUnload(lib);
+          return cuda_fail(e, "cudaFuncGetAttributes");
+        }
+        spills = spills || fa.localSizeBytes > kLmMaxSpillBytes;
+      }
     }
+    if (spills && t == 0) {
+      cudaLibraryUnload(lib);
+      continue;
+    }
+    for (int i = 0; i < K_COUNT; ++i)
+      if (group_of(i) == g) ft->k[i] = ks[i];
+    ft->lib[g] = lib;
+    ft->lm_min_blocks[g] = tries[t];
+    if (!log.empty()) ft->log += log;
+    return PCGB_OK;
   }
-  for (int i = 0; i < K_COUNT; ++i)
-    if (group_of(i) == g) ft->k[i] = ks[i];
-  ft->lib[g] = lib;
-  if (!log.empty()) ft->log += log;
-  return PCGB_OK;
+  return fail(PCGB_ECOMPILE, "kernel group %d could not be loaded", g);
+}
+
+// Threads per block for an LM launch: kernels built with the occupancy hint
+// take at most kLmMaxThreads (the per-voxel results do not depend on it).
+int lm_block(const pcgb_fitter* ft, int slot, int block) {
+  if (block <= 0) block = kDefaultBlock;
+  if (is_lm_slot(slot) && ft->lm_min_blocks[group_of(slot)] > 0 && block > kLmMaxThreads) block = kLmMaxThreads;
+  return block;
 }
 
 // The kernel of a slot, its group compiled and loaded on first use.
@@ -410,8 +462,8 @@ int pcgb_fitter_compile(const char* model_source, const char* model_struct, int 
   for (int g = 0; g < kGroups; ++g) {
     std::vector<char> cubin;
     std::string log;
-    if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, g, cubin,
-                           log))
+    if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, g,
+                           g == 1 ? 0 : kLmMinBlocks, cubin, log))
       return rc;
     all += log;
   }
@@ -712,6 +764,7 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
     if (block > kMaxBlock || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to %d", kMaxBlock);
     cudaKernel_t kq = nullptr;
     if (int rc = kernel_of(ft, q, &kq)) return rc;
+    block = lm_block(ft, q, block);
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     cudaError_t e = cudaMemsetAsync(work_counter, 0, sizeof(uint32_t), st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");

@@ -166,6 +166,18 @@ class WarmStartFitter:
         caller.wait_stream(s_out)
         return total
 
+    def _warm_check(self, solm, data, pars, b):
+        """The fallback check as its own kernel (pcgb_warm_check)."""
+        w = self.w
+        pv, plen = solm._proto_args()
+        rc = _lib.lib().pcgb_warm_check(
+            solm.build().handle, _p(solm.consts_t), solm._cstride, _p(data), _p(solm.lower_bound_t),
+            _p(solm.upper_bound_t), solm._bstride, pv, plen, _dvec(solm._lb_host) if solm._bstride == 0 else None,
+            _dvec(solm._ub_host) if solm._bstride == 0 else None, _dvec(w.init_values), 5.0, _p(pars),
+            _p(solm.lam_t), _p(solm.step_type_t), _p(solm.f_t), _p(b["cost"]), _p(b["backup"]), _p(b["cost_b"]),
+            _p(b["idx"]), _p(b["counts"]), data.shape[1], _stream())
+        _lib.check("pcgb_warm_check", rc)
+
     def _buffers(self, P: int, N: int, dev):
         key = (P, N, str(dev))
         if getattr(self, "_buf_key", None) != key:
@@ -178,16 +190,18 @@ class WarmStartFitter:
         return self._buf
 
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
-            lam0: float = 1e-3, timings: dict | None = None, fused="epilogue", events: list | None = None):
+            lam0: float = 1e-3, timings: dict | None = None, fused="select", events: list | None = None):
         """Warm-started fit of data (M, N); returns a WarmFit.
 
-        ``fused="epilogue"`` (default) runs the fallback check as the epilogue
-        of the warm LM launch and the select as the epilogue of the refit
-        launch (the flagged count never returns to the host, the signals are
-        read once); ``fused=True`` runs check, refit and select as three
+        ``fused="select"`` (default) runs the fallback check as its own kernel
+        and the select as the epilogue of the refit launch;
+        ``fused="epilogue"`` also runs the check as the epilogue of the warm
+        LM launch (the signals are read once, but the LM kernel then holds
+        more registers); ``fused=True`` runs check, refit and select as three
         kernels of their own; ``fused=False`` as the separate pipeline kernels
         (cost, constant start, cost, flags, prepare, refit, cost, select).
-        All three give the same results.
+        The flagged count never returns to the host except with
+        ``fused=False``. All give the same results.
         ``timings`` (a dict) receives per-stage milliseconds (synchronises);
         ``events`` (a list) receives (stage, CUDA event) pairs recorded after
         each stage on the current stream, without synchronising.
@@ -214,13 +228,19 @@ class WarmStartFitter:
         solm.setup(pars, prot, data, lb, ub)
         solm.lam_t.fill_(lam0)
         mark("setup")
-        if fused == "epilogue":
-            # the check as the warm LM's epilogue, the select as the refit's
+        if fused in ("epilogue", "select"):
             b = self._buffers(P, N, dev)
-            solm.run_check(iters_warm, w.init_values, 5.0, b["cost"], b["backup"], b["cost_b"], b["idx"],
-                           b["counts"])
-            mark("lm_warm")
-            mark("check")
+            if fused == "epilogue":  # the check as the warm LM's epilogue
+                solm.run_check(iters_warm, w.init_values, 5.0, b["cost"], b["backup"], b["cost_b"], b["idx"],
+                               b["counts"])
+                mark("lm_warm")
+                mark("check")
+            else:
+                solm.run(iters_warm)
+                mark("lm_warm")
+                self._warm_check(solm, data, pars, b)
+                mark("check")
+            # the select as the refit's epilogue
             solm.run_select(iters_fallback, b["cost"], b["backup"], b["cost_b"], b["idx"], b["counts"])
             mark("refit")
             mark("select")
@@ -236,13 +256,7 @@ class WarmStartFitter:
             L = _lib.lib()
             prog = solm.build()
             pv, plen = solm._proto_args()
-            rc = L.pcgb_warm_check(prog.handle, _p(solm.consts_t), solm._cstride, _p(data), _p(solm.lower_bound_t),
-                                   _p(solm.upper_bound_t), solm._bstride, pv, plen,
-                                   _dvec(solm._lb_host) if solm._bstride == 0 else None,
-                                   _dvec(solm._ub_host) if solm._bstride == 0 else None, _dvec(w.init_values), 5.0,
-                                   _p(pars), _p(solm.lam_t), _p(solm.step_type_t), _p(solm.f_t), _p(b["cost"]),
-                                   _p(b["backup"]), _p(b["cost_b"]), _p(b["idx"]), _p(b["counts"]), N, _stream())
-            _lib.check("pcgb_warm_check", rc)
+            self._warm_check(solm, data, pars, b)
             mark("check")
             solm.run_subset(b["idx"], N, iters_fallback, schedule=self.refit_schedule, n_items_dev=b["counts"])
             mark("refit")

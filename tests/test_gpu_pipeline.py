@@ -85,7 +85,8 @@ def test_fallback_refits_flagged_voxels():
 
 @pytest.mark.parametrize("per_voxel_bounds,schedule,mode", [(False, "grid", True), (True, "grid", True),
                                                             (False, "refill", True), (False, "grid", "epilogue"),
-                                                            (True, "grid", "epilogue")])
+                                                            (True, "grid", "epilogue"), (False, "grid", "select"),
+                                                            (True, "grid", "select")])
 def test_fused_fallback_matches_separate_kernels(per_voxel_bounds, schedule, mode):
     """Check + refit + select as three fused kernels, or as the epilogues of
     the warm LM and the refit launches (no host read of the flagged count
