@@ -14,6 +14,7 @@
 #include <nvrtc.h>
 
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -386,6 +387,25 @@ int load_group(pcgb_fitter* ft, int g) {
   return fail(PCGB_ECOMPILE, "kernel group %d could not be loaded", g);
 }
 
+// Largest "N bytes spill stores" that ptxas reports for the register-capped
+// LM kernels in a compile log (0 if the log is empty, e.g. served from cache).
+size_t max_lm_spill_bytes(const std::string& log) {
+  size_t worst = 0;
+  for (int slot = 0; slot < K_COUNT; ++slot) {
+    if (!is_lm_slot(slot)) continue;
+    const std::string key = std::string("Function properties for ") + kKernelNames[slot] + "\n";
+    const size_t at = log.find(key);
+    if (at == std::string::npos) continue;
+    const size_t sp = log.find("bytes spill stores", at);
+    if (sp == std::string::npos) continue;
+    size_t b = log.rfind(',', sp);
+    b = b == std::string::npos ? at : b + 1;
+    const size_t n = std::strtoull(log.c_str() + b, nullptr, 10);
+    if (n > worst) worst = n;
+  }
+  return worst;
+}
+
 // Threads per block for an LM launch: kernels built with the occupancy hint
 // take at most kLmMaxThreads (the per-voxel results do not depend on it).
 int lm_block(const pcgb_fitter* ft, int slot, int block) {
@@ -466,6 +486,15 @@ int pcgb_fitter_compile(const char* model_source, const char* model_struct, int 
     if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, g,
                            g == 1 ? 0 : kLmMinBlocks, cubin, log))
       return rc;
+    // the register-capped LM kernels spill too much for this model: the
+    // runtime will load the uncapped build, so compile (and cache) it too
+    if (g != 1 && max_lm_spill_bytes(log) > kLmMaxSpillBytes) {
+      all += log;
+      log.clear();
+      if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, g, 0,
+                             cubin, log))
+        return rc;
+    }
     all += log;
   }
   if (log_buf && log_len) {

@@ -46,15 +46,26 @@ def _compile(gm, M, dt=0, sdt=1):
     return rc, buf.value.decode(), L.pcgb_last_error().decode()
 
 
-def test_nvrtc_compiles_ivim_for_sm103a_without_spills():
+def test_nvrtc_compiles_ivim_for_sm103a_within_spill_cap():
+    """The LM kernels for a shared protocol are built for 6 resident blocks
+    per SM; their spills stay under the 256-byte cap for the fp32-state builds,
+    and a build over the cap (the all-FP64 one) is followed by the uncapped
+    build, which does not spill."""
+    import re
     w = synth.ivim()
     gm = codegen.generate(w.expr, w.pars, w.consts)
     for dt, sdt in ((0, 1), (0, 0), (1, 1)):
         rc, log, err = _compile(gm, w.M, dt, sdt)
         assert rc == 0, err
-        if log:  # empty when served from the cubin cache
-            blk = log.split("Function properties for pcgb_lm_c1_b1")[1].split("Compiling")[0]
-            assert "0 bytes spill stores" in blk
+        if not log:  # served from the cubin cache
+            continue
+        blocks = log.split("Function properties for pcgb_lm_c1_b1\n")[1:]
+        spills = [int(re.search(r"(\d+) bytes spill stores", b).group(1)) for b in blocks]
+        assert spills, log[:400]
+        if dt == 0:
+            assert spills[0] <= 256, spills
+        if spills[0] > 256:
+            assert len(spills) >= 2 and spills[1] == 0, spills
 
 
 def test_compile_errors_are_reported():
