@@ -387,6 +387,21 @@ def warm_headline(args, ws, rank, local, dev):
     med_p, frac_p = _median_rel_gpu(p_plain, ref)
     pp_p = _per_param_median(p_plain, ref)
 
+    # ---- the reference's own data-driven start (the IVIM notebook's segmented
+    # log-linear fits: b <= 100 and b >= 193 s/mm^2), same fixed bounds ---------
+    def run_seg(k):
+        p0, _, _ = pipeline.ivim_segmented_init(data, w.protocol, (0, 9), (10, 16), w.lb, w.ub, bounds=False)
+        pars.copy_(p0)
+        plain.setup(pars, list(w.protocol), data, list(w.lb), list(w.ub))
+        plain.run(k)
+        return pars
+
+    k_seg, curve_seg = budget_for_tolerance(run_seg, ref, range(0, 31))
+    seg = {"iters_for_1e-4": k_seg, "curve": {k: v[0] for k, v in curve_seg.items()}}
+    if k_seg is not None:
+        seg_ms = max_over_ranks([_time_ms(lambda: run_seg(k_seg), warmup=1, reps=args.steps)], device=dev)[0]
+        seg.update({"fits_per_s": ws * N / (seg_ms / 1e3), "ms_per_step": seg_ms})
+
     # ---- end to end through the public API from pinned host buffers ---------
     # WarmStartFitter.fit_host streams the voxels through the GPU in chunks:
     # every step copies all signals in and all fitted parameters out, with
@@ -422,7 +437,7 @@ def warm_headline(args, ws, rank, local, dev):
             "plain_curve": {k: v[0] for k, v in curve_plain.items()},
             "warm_accuracy": {"median_rel_err": med_w, "frac_voxels_gt_1e-4": frac_w, "per_param_median": pp_w},
             "plain_accuracy": {"median_rel_err": med_p, "frac_voxels_gt_1e-4": frac_p, "per_param_median": pp_p},
-            "fallback_voxels": n_fb, "refits_kept": n_kept,
+            "fallback_voxels": n_fb, "refits_kept": n_kept, "segmented_init_lm": seg,
             "stage_ms": {k: round(v, 3) for k, v in stages.items()},
             "accuracy_reference": "all-FP64 GPU fit, same LM, constant start, 300 iterations, tol 1e-30",
         },
