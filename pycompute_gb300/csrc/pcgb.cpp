@@ -755,8 +755,9 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
                                              : (bounds_stride == 0 ? K_LM_C0_B1 : K_LM_C0_B0);
   if (fb) {
     if (nprobs > (int64_t(1) << 31) - 1) return fail(PCGB_ERANGE, "the fallback indexes voxels with int32");
-    if (!fb->fb_count || !fb->fb_idx || !fb->cost || !fb->pars_backup || !fb->cost_backup)
-      return fail(PCGB_EINVAL, "fallback buffers (cost, backups, fb_idx, fb_count) are required");
+    if (!fb->fb_count) return fail(PCGB_EINVAL, "fb_count is required");
+    if (nprobs > 0 && (!fb->fb_idx || !fb->cost || !fb->pars_backup || !fb->cost_backup))
+      return fail(PCGB_EINVAL, "fallback buffers (cost, backups, fb_idx) are required");
     prm.cost = fb->cost;
     prm.pars_backup = fb->pars_backup;
     prm.cost_backup = fb->cost_backup;

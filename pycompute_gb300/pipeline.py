@@ -119,6 +119,8 @@ class WarmStartFitter:
         if tuple(out_h.shape) != (P, N) or data_h.dtype != torch.float32 or out_h.dtype != torch.float32:
             raise ValueError("data_h must be (M, N) and out_h (P, N) float32")
         dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        if N == 0:
+            return torch.zeros(2, dtype=torch.int32, device=dev)
         chunks = max(1, min(int(chunks), (N + 127) // 128))
         n_c = (N + chunks - 1) // chunks
         n_c = (n_c + 127) // 128 * 128

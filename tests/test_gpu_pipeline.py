@@ -133,6 +133,17 @@ def test_fit_host_streams_chunks_with_fit_results(N, chunks):
     assert int(counts[0]) == n_ref
 
 
+def test_warm_fit_of_zero_voxels():
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, DEV, seed=5)
+    wf = pipeline.WarmStartFitter(w, net)
+    data = torch.empty((16, 0), device=DEV)
+    res = wf.fit(data, iters_warm=2, iters_fallback=8)
+    counts = wf.fit_host(torch.empty((16, 0)).pin_memory(), torch.empty((4, 0)).pin_memory(), 2, 8)
+    torch.cuda.synchronize()
+    assert res.pars.shape == (4, 0) and res.n_fallback == 0 and int(counts.sum()) == 0
+
+
 def test_trained_network_beats_plain_lm_at_equal_iterations():
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     # training set: signals and the plain LM's fits of them as labels
