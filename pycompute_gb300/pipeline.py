@@ -168,6 +168,67 @@ class WarmStartFitter:
         caller.wait_stream(s_out)
         return total
 
+    def fit_stream(self, volumes, iters_warm: int, iters_fallback: int, lam0: float = 1e-3, device=None):
+        """Warm-started fits of a sequence of host-resident volumes.
+
+        volumes: iterable of (data_h (M, N), out_h (P, N)) float32 host tensors
+        (pinned, so the copies overlap the fits; N may differ between
+        volumes). Two device slots alternate: while volume i is fitted, volume
+        i+1 is copied in and volume i-1's parameters are copied back, so in
+        steady state each volume costs its fit alone. Every volume's result
+        equals fit()'s. Returns the device int32 tensor [fallback voxels,
+        refits kept] summed over volumes; the caller's stream waits for the
+        last copy back.
+        """
+        dev = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        P = self.w.P
+        if getattr(self, "_stream_key", None) != str(dev):
+            self._streams3 = [torch.cuda.Stream(device=dev) for _ in range(3)]
+            self._stream_slots = [{}, {}]
+            self._stream_key = str(dev)
+        s_in, s_fit, s_out = self._streams3
+        caller = torch.cuda.current_stream(dev)
+        for st in (s_in, s_fit, s_out):
+            st.wait_stream(caller)
+        total = torch.zeros(2, dtype=torch.int32, device=dev)
+        total.record_stream(s_fit)
+        ev_fit, ev_out = [], []
+        for i, (data_h, out_h) in enumerate(volumes):
+            M, N = data_h.shape
+            if tuple(out_h.shape) != (P, N) or data_h.dtype != torch.float32 or out_h.dtype != torch.float32:
+                raise ValueError("each volume needs data (M, N) and out (P, N) float32 host tensors")
+            slot = self._stream_slots[i % 2]
+            if slot.get("shape") != (M, N):
+                with torch.cuda.stream(s_in):  # the slot's previous buffers are released on s_in's order
+                    slot.update(shape=(M, N), data=torch.empty((M, N), dtype=torch.float32, device=dev),
+                                pars=torch.empty((P, N), dtype=torch.float32, device=dev))
+            d, p = slot["data"], slot["pars"]
+            d.record_stream(s_fit)  # the allocator may reuse the slots only after these streams' work
+            p.record_stream(s_fit)
+            p.record_stream(s_out)
+            ev_in = torch.cuda.Event()
+            with torch.cuda.stream(s_in):
+                if i >= 2:
+                    s_in.wait_event(ev_fit[i - 2])  # the slot's signals are no longer read
+                d.copy_(data_h, non_blocking=True)
+                ev_in.record(s_in)
+            with torch.cuda.stream(s_fit):
+                s_fit.wait_event(ev_in)
+                if i >= 2:
+                    s_fit.wait_event(ev_out[i - 2])  # the slot's parameters are copied out
+                res = self.fit(d, iters_warm, iters_fallback, pars_out=p, lam0=lam0)
+                total.add_(res.counts)
+                ev_fit.append(torch.cuda.Event())
+                ev_fit[-1].record(s_fit)
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(ev_fit[-1])
+                out_h.copy_(p, non_blocking=True)
+                ev_out.append(torch.cuda.Event())
+                ev_out[-1].record(s_out)
+        caller.wait_stream(s_fit)
+        caller.wait_stream(s_out)
+        return total
+
     def _warm_check(self, solm, data, pars, b):
         """The fallback check as its own kernel (pcgb_warm_check)."""
         w = self.w
@@ -189,6 +250,10 @@ class WarmStartFitter:
                              idx=torch.empty(N, dtype=torch.int32, device=dev),
                              counts=torch.zeros(2, dtype=torch.int32, device=dev))
             self._buf_key = key
+        # used on the current stream: replaced buffers are not reused before its work ends
+        st = torch.cuda.current_stream(dev)
+        for t in self._buf.values():
+            t.record_stream(st)
         return self._buf
 
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,

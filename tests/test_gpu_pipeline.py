@@ -133,6 +133,26 @@ def test_fit_host_streams_chunks_with_fit_results(N, chunks):
     assert int(counts[0]) == n_ref
 
 
+def test_fit_stream_volumes_with_fit_results():
+    """fit_stream (volumes double-buffered, copies overlapping fits) gives each
+    volume the result of fit() on it."""
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, DEV, seed=5)
+    true, d0 = pipeline.synth_gpu(w, 70001, seed=13, device=DEV)
+    net.fit_normalisation(d0, true)
+    wf = pipeline.WarmStartFitter(w, net)
+    vols, refs = [], []
+    for k, n in enumerate((70001, 1000, 70001, 4099)):
+        _, d = pipeline.synth_gpu(w, n, seed=20 + k, device=DEV)
+        refs.append(wf.fit(d, iters_warm=2, iters_fallback=8).pars.cpu().numpy().copy())
+        vols.append((d.cpu().pin_memory(), torch.full((w.P, n), float("nan")).pin_memory()))
+    counts = wf.fit_stream(vols, iters_warm=2, iters_fallback=8)
+    torch.cuda.synchronize()
+    for (_, out), ref in zip(vols, refs):
+        np.testing.assert_array_equal(out.numpy(), ref)
+    assert int(counts[0]) >= 0
+
+
 def test_warm_fit_of_zero_voxels():
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, DEV, seed=5)
