@@ -160,11 +160,13 @@ def _median_rel_np(a, b):
     return float(np.median(r)), float(np.mean(r > TOL))
 
 
-def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 30):
+def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 30, plan: dict | None = None):
     """The reference algorithm (plain LM, fp32) on the host cores, on IVIM-16
     at the smallest iteration budget whose median error against the all-FP64
     CPU fit (same LM, constant start, 300 iterations) is <= 1e-4. The sample
     grows until one fit takes at least target_s / 4; that size is timed once.
+    With ``plan`` (the result of an earlier call) the budget and the sample
+    size are reused and only the timed fit runs again.
     """
     from oracle import OracleModel, RefIVIM, ref_available
     from pycompute_gb300 import synth
@@ -177,6 +179,14 @@ def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 3
         impl, kind = RefIVIM(M_IVIM16), "reference"
     else:
         impl, kind = port, "port"
+    if plan is not None:
+        k_run, curve, n = plan["iters"], plan["curve"], plan["n"]
+        _, data, init, lb, ub, prot = w.generate(n, seed=8)
+        p = init.copy()
+        t0 = time.perf_counter()
+        impl.lm_run(p, prot, data, lb, ub, k_run)
+        el = time.perf_counter() - t0
+        return dict(plan, value=n / el, sample=plan["sample"].rsplit(", ", 1)[0] + f", {el:.2f} s")
     _, data, init, lb, ub, prot = w.generate(n_ref, seed=7)
     p64 = init.astype(np.float64)
     port.lm_run(p64, prot.astype(np.float64), data.astype(np.float64), lb.astype(np.float64),
@@ -204,7 +214,7 @@ def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 3
     sample = (f"{n} IVIM-16 voxels x {k_run} iterations (the 1e-4 budget on {n_ref} voxels vs the all-FP64 CPU fit; "
               f"{what}, {cores} threads), {el:.2f} s")
     return {"value": n / el, "unit": "fits/s", "cores": cores, "kind": kind, "sample": sample, "iters": k_run,
-            "curve": curve}
+            "curve": curve, "n": n}
 
 
 def cpu_parity_ivim10(n: int = 1 << 18, iters: int = 100):
@@ -714,9 +724,12 @@ def run_reference_arm(args):
     ws, rank, local = _dist()
     if rank != 0:
         return 0
-    vals, last = [], None
+    # the budget and the sample size are settled once; every step then times
+    # one bounded fit of the sample (about cpu_seconds / 4 of host time)
+    plan = cpu_reference_at_tol(target_s=args.cpu_seconds)
+    vals, last = [], plan
     for s in range(args.warmup + args.steps):
-        last = cpu_reference_at_tol(target_s=args.cpu_seconds)
+        last = cpu_reference_at_tol(target_s=args.cpu_seconds, plan=plan)
         if s >= args.warmup:
             vals.append(last["value"])
     value = statistics.median(vals)
