@@ -328,11 +328,9 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
   const double delta = abs_bits(gn) > 0x3FF0000000000000ULL ? 4e-16 * gn : 4e-16;
 
   double inv_d[P];
-  double Lr[P][P];
+  double Lr[P][P];  // L_ij = c_ij / d_j (j < i), formed once when d_j is known
 #pragma unroll
   for (int j = 0; j < P; ++j) {
-#pragma unroll
-    for (int q = 0; q < j; ++q) Lr[j][q] = c[j][q] * inv_d[q];
 #pragma unroll
     for (int i = j + 1; i < P; ++i) {
       double t = c[i][j];
@@ -354,7 +352,10 @@ PCGB_HD void gmw81_solve_f32in_f64(const float (&A)[P * (P + 1) / 2], const floa
     }
     inv_d[j] = rcp64(d);
 #pragma unroll
-    for (int i = j + 1; i < P; ++i) c[i][i] = fma(-c[i][j], c[i][j] * inv_d[j], c[i][i]);
+    for (int i = j + 1; i < P; ++i) {
+      Lr[i][j] = c[i][j] * inv_d[j];
+      c[i][i] = fma(-c[i][j], Lr[i][j], c[i][i]);
+    }
   }
   // L D y = b' with L_ij d_j = c_ij, then L^T z = y (solver.py:298-308, 341-350)
 #pragma unroll
