@@ -331,7 +331,7 @@ def warm_headline(args, ws, rank, local, dev):
     net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, dev, seed=77)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    net.train(tr, lab, epochs=args.warm_epochs, batch=8192, lr=2e-3)
+    net.train(tr, lab, epochs=args.warm_epochs, batch=8192, lr=args.warm_lr)
     torch.cuda.synchronize()
     train_s = time.perf_counter() - t1
     del tr, lab, s
@@ -455,7 +455,7 @@ def warm_headline(args, ws, rank, local, dev):
         "stages": stages, "clocks": clk.summary(), "h2d": data_h.nbytes, "d2h": outs[0].nbytes,
         "k_warm": k_warm, "k_plain": k_plain, "e2e_same": e2e_same, "e2e_chunks": args.e2e_chunks,
         "detail": {
-            "train_voxels": args.warm_train, "epochs": args.warm_epochs, "train_s": round(train_s, 3),
+            "train_voxels": args.warm_train, "epochs": args.warm_epochs, "lr": args.warm_lr, "train_s": round(train_s, 3),
             "setup_s": round(setup_s, 1), "lam0": lam0,
             "warm_curve": {k: v[0] for k, v in curve_warm.items()},
             "plain_curve": {k: v[0] for k, v in curve_plain.items()},
@@ -762,7 +762,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--warm-voxels", type=int, default=1 << 24)
-    ap.add_argument("--warm-epochs", type=int, default=64)
+    ap.add_argument("--warm-epochs", type=int, default=128)
+    ap.add_argument("--warm-lr", type=float, default=8e-3, help="peak Adam learning rate (cosine decay)")
     ap.add_argument("--warm-lam0", type=float, default=3e-3)
     ap.add_argument("--warm-train", type=int, default=1 << 21)
     ap.add_argument("--e2e-chunks", type=int, default=8, help="voxel chunks of the streamed end-to-end fit")

@@ -402,7 +402,11 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
     for (int k = 0; k < P; ++k) g[k] = hd[k] = TA(0);
 #pragma unroll
     for (int k = 0; k < H; ++k) h[k] = TA(0);
-#pragma unroll
+    // The sample loops stay rolled: unrolled over 16 samples the iteration no
+    // longer fits the instruction cache (measured on IVIM-16, 8.4 M voxels x 8
+    // iterations: 13.7 ms unrolled, 11.7 ms rolled; IVIM-10 x 20: 30.3 -> 28.3
+    // ms); the samples then sit in L1-cached local memory.
+#pragma unroll 1
     for (int i = 0; i < M; ++i) {
       TA c[C > 0 ? C : 1];
 #pragma unroll
@@ -484,7 +488,7 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
 #pragma unroll
     for (int k = 0; k < P; ++k) pt[k] = p[k] - stp[k];
     TA ftp = TA(0);
-#pragma unroll
+#pragma unroll 1
     for (int i = 0; i < M; ++i) {
       TA c[C > 0 ? C : 1];
 #pragma unroll

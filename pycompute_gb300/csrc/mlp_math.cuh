@@ -3,7 +3,6 @@
 #pragma once
 
 #include <cuda_bf16.h>
-#include <cuda_fp16.h>
 
 #include <cstdint>
 
@@ -18,35 +17,39 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
 // GELU in its tanh form (Hendrycks & Gimpel 2016),
 //   gelu(z) = z/2 (1 + tanh(u)),  u = sqrt(2/pi) (z + 0.044715 z^3),
 // and its derivative 1/2 (1 + t) + z/2 (1 - t^2) sqrt(2/pi) (1 + 3 * 0.044715 z^2).
-// t = tanh(u) is evaluated for two pre-activations at once: u = z (c + c' z^2)
-// in f16x2 arithmetic (c = sqrt(2/pi), c' = 0.044715 c; an overflow to +-Inf
-// saturates t to +-1 as it should) and tanh by one tanh.approx.f16x2 MUFU
-// operation. Its error (~2^-10 relative, like tanh.approx.f32) is below the
-// bf16 rounding of the activation; the rest of the GELU stays in fp32. Every
-// kernel (training epilogues and both inference kernels) uses this one
-// function, so training and inference see the same activation.
-__device__ __forceinline__ float2 gelu_tanh2(float z0, float z1) {
-  const __half2 z = __floats2half2_rn(z0, z1);
-  const __half2 q = __hfma2(__hmul2(z, z), __float2half2_rn(0.0356774081363001f), __float2half2_rn(0.7978845608028654f));
-  const __half2 u = __hmul2(z, q);
-  uint32_t ti;
-  asm("tanh.approx.f16x2 %0, %1;" : "=r"(ti) : "r"(*reinterpret_cast<const uint32_t*>(&u)));
-  return __half22float2(*reinterpret_cast<const __half2*>(&ti));
+// Evaluated for two pre-activations at once in bf16x2 arithmetic, the format
+// the next layer consumes: z rounded to bf16, u = z (c + c' z^2) with
+// c = bf16(sqrt(2/pi)), c' = bf16(0.044715 sqrt(2/pi)) (each product and the
+// fused multiply-add rounded to bf16; an overflow to +-Inf saturates t to
+// +-1), t = tanh.approx.bf16x2(u) (one MUFU operation per element), and
+// 2 gelu(z) = z t + z by one fused bf16x2 multiply-add. Seven instructions per
+// pair of activations; the roundings are those of the bf16 operands the
+// tensor cores read anyway. Every kernel (training epilogues and both
+// inference kernels) uses these functions, so training and inference see the
+// same activation.
+__device__ __forceinline__ uint32_t bf162_bits(__nv_bfloat162 v) { return *reinterpret_cast<uint32_t*>(&v); }
+__device__ __forceinline__ __nv_bfloat162 bits_bf162(uint32_t v) { return *reinterpret_cast<__nv_bfloat162*>(&v); }
+__device__ __forceinline__ __nv_bfloat162 tanh_bf16x2(__nv_bfloat162 z) {
+  const __nv_bfloat162 c = __float2bfloat162_rn(0.7978845608028654f);
+  const __nv_bfloat162 c3 = __float2bfloat162_rn(0.0356774081363001f);
+  const __nv_bfloat162 u = __hmul2(z, __hfma2(__hmul2(z, z), c3, c));
+  uint32_t t;
+  asm("tanh.approx.bf16x2 %0, %1;" : "=r"(t) : "r"(bf162_bits(u)));
+  return bits_bf162(t);
 }
-__device__ __forceinline__ float gelu(float z) {
-  const float t = gelu_tanh2(z, z).x;
-  const float h = 0.5f * z;
-  return fmaf(h, t, h);
-}
-// bf16 pair of 2 gelu(z): exactly twice the bf16 rounding of gelu(z), for a
-// next layer whose weights are stored halved (the products are unchanged)
+// bf16 pair of 2 gelu(z0), 2 gelu(z1), for a next layer whose weights are
+// stored halved (the products are those of gelu with the full weights)
 __device__ __forceinline__ uint32_t gelu2x_pack_bf16(float z0, float z1) {
-  const float2 t = gelu_tanh2(z0, z1);
-  return pack_bf16(fmaf(z0, t.x, z0), fmaf(z1, t.y, z1));
+  const __nv_bfloat162 z = __floats2bfloat162_rn(z0, z1);
+  return bf162_bits(__hfma2(z, tanh_bf16x2(z), z));
+}
+// gelu(z) of the same recipe: half of 2 gelu(z), exact in bf16
+__device__ __forceinline__ float gelu(float z) {
+  return 0.5f * __low2float(bits_bf162(gelu2x_pack_bf16(z, z)));
 }
 __device__ __forceinline__ float gelu_grad(float z) {
   const float z2 = z * z;
-  const float t = gelu_tanh2(z, z).x;
+  const float t = __low2float(tanh_bf16x2(__float2bfloat162_rn(z)));
   return fmaf(0.5f, t, 0.5f) + 0.5f * z * (1.0f - t * t) * fmaf(0.1070322244089003f, z2, 0.7978845608028654f);
 }
 // eight bf16 values times 1/2 (exact for normal numbers)
@@ -61,9 +64,11 @@ __device__ __forceinline__ uint4 halve_bf16x8(uint4 v) {
 }
 
 // Network input of one sample: s / max, or log(max(s / max, 1e-6)) with log_in.
+// The input is rounded to bf16 right after, so the fast logarithm (__logf,
+// absolute error ~2^-21 here) loses nothing the rounding keeps.
 __device__ __forceinline__ float input_transform(float s, float inv, int log_in) {
   const float x = s * inv;
-  return log_in ? logf(fmaxf(x, 1e-6f)) : x;
+  return log_in ? __logf(fmaxf(x, 1e-6f)) : x;
 }
 
 }  // namespace pcgb_mlp

@@ -49,7 +49,11 @@ constexpr int THREADS = NWG * 128;
 constexpr int TMEM_COLS = 512;  // >= NWG x 128 accumulator columns, a power of 2
 constexpr int LDH_G = HID + 8;  // leading dimension of the hidden weights in global memory
 constexpr int LD1_G = NIN + 8;  // ... of the first layer's weights
-constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait counts as lost
+constexpr unsigned kWaitLimit = 1u << 20;  // try_wait rounds before a wait counts as lost
+// Longest time one try_wait round may keep the thread suspended (ns); the
+// thread resumes as soon as the phase completes, so the hint only bounds how
+// often a waiting warp comes back to poll instead of taking issue slots.
+constexpr unsigned kSuspendNs = 20000;
 
 // The biases enter the accumulators through one more MMA per layer: A = a
 // 128 x 16 tile whose first two columns are 1, B = the layer's bias split
@@ -135,36 +139,31 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
   for (unsigned i = 0; i < kWaitLimit; ++i) {
     uint32_t done;
     asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(mbar), "r"(parity)
+        : "r"(mbar), "r"(parity), "n"(kSuspendNs)
         : "memory");
     if (done) return true;
   }
   return false;
 }
 
-// Start loading 32 consecutive fp32 accumulator columns of this thread's TMEM
-// lane; the registers are valid only after tmem_wait32 on the same array.
-__device__ __forceinline__ void tmem_ld32_start(uint32_t taddr, uint32_t (&r)[32]) {
+// Start loading 16 consecutive fp32 accumulator columns of this thread's TMEM
+// lane; the registers are valid only after tmem_wait16 on the same array.
+__device__ __forceinline__ void tmem_ld16_start(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,"
-      "%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
 // Wait for every outstanding tcgen05.ld of this thread; the registers of r are
 // read-write operands, so no use of them can be scheduled before the wait.
-__device__ __forceinline__ void tmem_wait32(uint32_t (&r)[32]) {
+__device__ __forceinline__ void tmem_wait16(uint32_t (&r)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;"
                : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
                  "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
-                 "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
-                 "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
-                 "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+                 "+r"(r[15])
                :
                : "memory");
 }
@@ -195,12 +194,11 @@ __device__ void stage_weights(bf16* dst, const bf16* src, int rows, int rows_liv
   }
 }
 
-// 2 GELU of 32 pre-activations (columns [c0, c0 + 32), bias included), written
-// as bf16 into row r of the next layer's A operand
-__device__ __forceinline__ void gelu_row_chunk(const uint32_t (&acc)[32], int c0, bf16* act, int r) {
-  unsigned char* base = reinterpret_cast<unsigned char*>(act);
+// 2 GELU of 16 pre-activations (columns [c0, c0 + 16), bias included), written
+// as bf16 into row r of the next layer's A operand (row_base = its byte offset)
+__device__ __forceinline__ void gelu_row16(const uint32_t (&acc)[16], int c0, unsigned char* row_base) {
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
+  for (int q = 0; q < 2; ++q) {
     uint4 o;
     uint32_t* w = reinterpret_cast<uint32_t*>(&o);
 #pragma unroll
@@ -208,7 +206,7 @@ __device__ __forceinline__ void gelu_row_chunk(const uint32_t (&acc)[32], int c0
       const int j = q * 8 + 2 * e;
       w[e] = pcgb_mlp::gelu2x_pack_bf16(__uint_as_float(acc[j]), __uint_as_float(acc[j + 1]));
     }
-    *reinterpret_cast<uint4*>(base + core_off(r, c0 + q * 8, HID)) = o;
+    *reinterpret_cast<uint4*>(row_base + ((c0 + q * 8) >> 3) * 128) = o;
   }
 }
 
@@ -348,12 +346,20 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
       }
       fence_after_sync();
       if (layer < 3) {
-#pragma unroll 1
-        for (int c = 0; c < HID / 32; ++c) {
-          uint32_t acc[32];
-          tmem_ld32_start(t_row + uint32_t(c * 32), acc);
-          tmem_wait32(acc);
-          gelu_row_chunk(acc, c * 32, S.act[g], r);
+        // 16 columns at a time, the next chunk's TMEM load in flight while
+        // this chunk's GELU runs
+        unsigned char* row_base = reinterpret_cast<unsigned char*>(S.act[g]) + core_off(r, 0, HID);
+        uint32_t a0[16], a1[16];
+        tmem_ld16_start(t_row, a0);
+        tmem_wait16(a0);
+#pragma unroll
+        for (int c = 0; c < HID / 16; c += 2) {
+          tmem_ld16_start(t_row + uint32_t((c + 1) * 16), a1);
+          gelu_row16(a0, c * 16, row_base);
+          tmem_wait16(a1);
+          if (c + 2 < HID / 16) tmem_ld16_start(t_row + uint32_t((c + 2) * 16), a0);
+          gelu_row16(a1, (c + 1) * 16, row_base);
+          if (c + 2 < HID / 16) tmem_wait16(a0);
         }
       } else {
         float y[16];

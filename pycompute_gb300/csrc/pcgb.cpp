@@ -116,9 +116,10 @@ bool is_lm_slot(int slot) {
 constexpr int kLmMinBlocks = 6;
 constexpr int kLmMaxThreads = 128;
 // Spilled words stay in L1 and cost less than the occupancy gain up to a few
-// hundred bytes per thread (measured: 5 -> 6 blocks per SM, 0 -> ~100 bytes
-// of spills, IVIM-10 +2.6 %, IVIM-16 +0.7 %; 7 blocks loses on IVIM-16); past
-// this the cap is dropped.
+// hundred bytes per thread (measured with the sample loops rolled, 8.4 M
+// voxels: 5 -> 6 blocks per SM, 0 -> 84 bytes of spills, IVIM-16 x 8
+// iterations 11.86 -> 11.68 ms, IVIM-10 x 20 flat; 7 and 8 blocks within 1 %);
+// past this the cap is dropped.
 constexpr size_t kLmMaxSpillBytes = 256;
 
 std::string program_source(const char* model_source, const char* model_struct, int P, int C, int M, int dtype,
