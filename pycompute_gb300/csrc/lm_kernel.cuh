@@ -501,19 +501,22 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
     bool accept, very_good, pred_neg;
     if constexpr (kMixed<TA, TS>) {
       // predicted = s.g - s^T h s / 2 and the test rho = actual / predicted > mu
-      // evaluated without the division: for predicted > 0 it is
-      // actual > mu * predicted; predicted == +0 gives rho = +Inf.
-      // actual = (f - ftp) / 2 is exact in FP64, so its sign is the sign of f - ftp
-      const double actual = 0.5 * (widen(f) - widen(ftp));
+      // with actual = (f - ftp) / 2, evaluated without the division and with
+      // the halving moved to the thresholds: for predicted > 0 it is
+      // f - ftp > 2 mu predicted; predicted == +0 gives rho = +Inf.
+      // f - ftp is exact in FP64, so its sign is the sign of f - ftp.
+      // s^T h s = sum_i s_i (h_ii s_i + 2 sum_{j<i} h_ij s_j), the doubled
+      // off-diagonal terms taken from 2 h_ij (exact in fp32).
+      const double actual2 = widen(f) - widen(ftp);
       double sg = 0.0, q = 0.0, sd[P];
 #pragma unroll
       for (int i = 0; i < P; ++i) sd[i] = widen(stp[i]);
 #pragma unroll
       for (int i = 0; i < P; ++i) {
-        double off = 0.0;
+        double off2 = 0.0;
 #pragma unroll
-        for (int j = 0; j < i; ++j) off = fma(widen(h[pk(i, j)]), sd[j], off);
-        const double ti = fma(2.0, off, widen(h[pk(i, i)]) * sd[i]);
+        for (int j = 0; j < i; ++j) off2 = fma(widen(2.0f * h[pk(i, j)]), sd[j], off2);
+        const double ti = fma(widen(h[pk(i, i)]), sd[i], off2);
         q = fma(sd[i], ti, q);
         sg = fma(sd[i], widen(g[i]), sg);
       }
@@ -521,13 +524,13 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
       // comparisons on bit patterns (integer pipe): for positive doubles the
       // order of the bits is the order of the values
       const long long pb = __double_as_longlong(pred);
-      const long long ab = __double_as_longlong(actual);
+      const long long ab = __double_as_longlong(actual2);
       const bool pzero = pb == 0;                         // +0: rho = +Inf
       const bool pos = pb > 0 && pb < 0x7ff0000000000000LL;  // finite, > +0
       const bool up = f > ftp;                            // actual > 0
-      accept = up && ((pos && ab > __double_as_longlong(widen(mu) * pred)) || pzero);
+      accept = up && ((pos && ab > __double_as_longlong(widen(2.0f * mu) * pred)) || pzero);
       // only read when accept holds: then actual > 0 and pred > 0 or +0
-      very_good = pzero || ab > __double_as_longlong(widen(eta) * pred);
+      very_good = pzero || ab > __double_as_longlong(widen(2.0f * eta) * pred);
       // pred < 0: sign bit set, magnitude in (0, Inf]
       pred_neg = static_cast<unsigned long long>(pb) > 0x8000000000000000ULL &&
                  static_cast<unsigned long long>(pb) <= 0xfff0000000000000ULL;

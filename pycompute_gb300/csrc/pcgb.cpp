@@ -275,6 +275,30 @@ int launch(pcgb_fitter* ft, KernelSlot slot, PcgbLmParams prm, int64_t n, int bl
   return PCGB_OK;
 }
 
+// launch() for work whose item count lives on the device (prm.n_items_dev,
+// at most n): the kernel strides over its items, so the grid holds only as
+// many blocks as are resident at once instead of one block per possible item
+// (the blocks past the count would each start only to exit).
+int launch_resident(pcgb_fitter* ft, KernelSlot slot, PcgbLmParams prm, int64_t n, int block, void* stream) {
+  cudaKernel_t kern = nullptr;
+  if (int rc = kernel_of(ft, slot, &kern)) return rc;
+  block = lm_block(ft, slot, block);
+  if (block > kMaxBlock || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to %d", kMaxBlock);
+  if (n == 0) return PCGB_OK;
+  int per_sm = 0, dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(kern), block, 0);
+  if (e != cudaSuccess || per_sm < 1) per_sm = 1;
+  int grid = grid_for(n, block);
+  if (int64_t(per_sm) * (sms > 0 ? sms : 1) < grid) grid = per_sm * (sms > 0 ? sms : 1);
+  void* args[] = {&prm};
+  e = cudaLaunchKernel(reinterpret_cast<const void*>(kern), dim3(grid), dim3(block), args, 0,
+                       static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, kKernelNames[slot]);
+  return PCGB_OK;
+}
+
 int fill_protocol(const pcgb_fitter* ft, PcgbLmParams& prm, int64_t cstride, int64_t n, const double* protocol,
                   int protocol_len) {
   if (cstride == 0) {
@@ -776,7 +800,7 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
     prm.vox_idx = fb->fb_idx;
     prm.n_items = nprobs;
     prm.n_items_dev = fb->fb_count;
-    return launch(ft, KernelSlot(slot + (K_LMS_C1_B1 - K_LM_C1_B1)), prm, nprobs, block, stream);
+    return launch_resident(ft, KernelSlot(slot + (K_LMS_C1_B1 - K_LM_C1_B1)), prm, nprobs, block, stream);
   }
   if (work_counter) {
     // refill schedule: persistent grid, warps claim 256-item chunks from the counter
@@ -820,6 +844,7 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
     prm.vox_idx = vox_idx;
     prm.n_items = n_items;
     prm.n_items_dev = n_items_dev;
+    if (n_items_dev) return launch_resident(ft, slot, prm, n_items, block, stream);
     return launch(ft, slot, prm, n_items, block, stream);
   }
   return launch(ft, slot, prm, nprobs, block, stream);
