@@ -83,6 +83,10 @@ template <> struct Num<float> {
   static PCGB_HD float slb(const PcgbLmParams& a, int k) { return a.shared_lb_f[k]; }
   static PCGB_HD float sub(const PcgbLmParams& a, int k) { return a.shared_ub_f[k]; }
   static PCGB_HD float inf() { return __int_as_float(0x7f800000); }
+  // tol, mu, eta, acc, dec (k = 0..4)
+  static PCGB_HD float lmc(const PcgbLmParams& a, int k) {
+    return k == 0 ? a.tol_f : k == 1 ? a.mu_f : k == 2 ? a.eta_f : k == 3 ? a.acc_f : a.dec_f;
+  }
 };
 template <> struct Num<double> {
   static PCGB_HD double gmw_eps() { return 4e-16; }   // solver.py:109
@@ -92,6 +96,9 @@ template <> struct Num<double> {
   static PCGB_HD double slb(const PcgbLmParams& a, int k) { return a.shared_lb_d[k]; }
   static PCGB_HD double sub(const PcgbLmParams& a, int k) { return a.shared_ub_d[k]; }
   static PCGB_HD double inf() { return __longlong_as_double(0x7ff0000000000000LL); }
+  static PCGB_HD double lmc(const PcgbLmParams& a, int k) {
+    return k == 0 ? a.tol : k == 1 ? a.mu : k == 2 ? a.eta : k == 3 ? a.acc : a.dec;
+  }
 };
 
 PCGB_HD constexpr int pk(int i, int j) { return i * (i + 1) / 2 + j; }  // packed lower index, j <= i
@@ -234,6 +241,12 @@ PCGB_HD void max_abs_bits(unsigned long long& m, double x) {
 }
 PCGB_HD double from_bits(unsigned long long b) { return __longlong_as_double(static_cast<long long>(b)); }
 
+// The hardware conversions for the rare inputs of widen and narrow, kept out
+// of line: an F2F issues on the FP64 pipe, and inlined into a call site the
+// compiler may predicate it into the common path as well.
+__device__ __noinline__ double widen_hw(float x) { return static_cast<double>(x); }
+__device__ __noinline__ float narrow_hw(double x) { return __double2float_rn(x); }
+
 // Exact float -> double widening on the integer pipe (the F2F instruction
 // issues on the FP64 pipe): rebias the exponent by 1023 - 127 = 896 and move
 // the 23-bit mantissa to the top of the 52-bit one. Zero keeps its sign;
@@ -246,7 +259,7 @@ PCGB_HD double widen(float x) {
     return __hiloint2double(static_cast<int>(hi), static_cast<int>(u << 29));
   }
   if ((u << 1) == 0u) return __hiloint2double(static_cast<int>(u & 0x80000000u), 0);
-  return static_cast<double>(x);
+  return widen_hw(x);
 }
 
 // Exact-rounding double -> float (to nearest, ties to even) on the integer
@@ -266,7 +279,7 @@ PCGB_HD float narrow(double x) {
     f += (rem > 0x10000000u || (rem == 0x10000000u && (f & 1u))) ? 1u : 0u;
     return __uint_as_float(f | (hi & 0x80000000u));
   }
-  return __double2float_rn(x);
+  return narrow_hw(x);
 }
 
 // 1/x in FP64 from a float seed and one third-order Newton-Raphson step
@@ -626,7 +639,8 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
   int st = a.step_type[v];
   TA f = load<TA>(a.f, v);
   TA first = f;
-  const TA tol = TA(a.tol), mu = TA(a.mu), eta = TA(a.eta), acc = TA(a.acc), dec = TA(a.dec);
+  const TA tol = Num<TA>::lmc(a, 0), mu = Num<TA>::lmc(a, 1), eta = Num<TA>::lmc(a, 2), acc = Num<TA>::lmc(a, 3),
+             dec = Num<TA>::lmc(a, 4);
   int done = 0;
 
   if constexpr (SHARED_C) {
@@ -717,7 +731,8 @@ struct VoxelFit {
   PCGB_HD bool finished(const PcgbLmParams& a) const { return st == 0 || it >= a.iters; }
 
   PCGB_HD void step(const PcgbLmParams& a) {
-    const TA tol = TA(a.tol), mu = TA(a.mu), eta = TA(a.eta), acc = TA(a.acc), dec = TA(a.dec);
+    const TA tol = Num<TA>::lmc(a, 0), mu = Num<TA>::lmc(a, 1), eta = Num<TA>::lmc(a, 2), acc = Num<TA>::lmc(a, 3),
+             dec = Num<TA>::lmc(a, 4);
     TA first_it = first;
     if constexpr (SHARED_C) {
       lm_iterate<Model, M, TA, TS>(SharedConsts<TA, M>{a}, d, p, lo, hi, stp, lam, st, f, first_it, done, 1, tol, mu,
@@ -1173,7 +1188,8 @@ __device__ void random_search_grid(const PcgbLmParams& a) {
       for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
     }
     TA bf = load<TA>(a.best_f, v);
-    const TA tol = TA(a.tol), mu = TA(a.mu), eta = TA(a.eta), acc = TA(a.acc), dec = TA(a.dec);
+    const TA tol = Num<TA>::lmc(a, 0), mu = Num<TA>::lmc(a, 1), eta = Num<TA>::lmc(a, 2), acc = Num<TA>::lmc(a, 3),
+             dec = Num<TA>::lmc(a, 4);
     for (int dr = 0; dr < a.iters; ++dr) {
       TA p[P], stp[P];
 #pragma unroll

@@ -36,6 +36,7 @@ struct PcgbLmParams {
   int iters;
   int flags;
   double tol, mu, eta, acc, dec;
+  float tol_f, mu_f, eta_f, acc_f, dec_f;  // the same constants rounded to float (set with them)
   // fallback check of a warm-started fit (warm_check_grid / warm_select_grid)
   const unsigned int* n_items_dev;  // when set, the work-item count is min(*n_items_dev, n_items)
   void* cost;                       // (N) cost at the fit's final point, out

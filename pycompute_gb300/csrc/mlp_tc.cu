@@ -49,11 +49,7 @@ constexpr int THREADS = NWG * 128;
 constexpr int TMEM_COLS = 512;  // >= NWG x 128 accumulator columns, a power of 2
 constexpr int LDH_G = HID + 8;  // leading dimension of the hidden weights in global memory
 constexpr int LD1_G = NIN + 8;  // ... of the first layer's weights
-constexpr unsigned kWaitLimit = 1u << 20;  // try_wait rounds before a wait counts as lost
-// Longest time one try_wait round may keep the thread suspended (ns); the
-// thread resumes as soon as the phase completes, so the hint only bounds how
-// often a waiting warp comes back to poll instead of taking issue slots.
-constexpr unsigned kSuspendNs = 20000;
+constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait counts as lost
 
 // The biases enter the accumulators through one more MMA per layer: A = a
 // 128 x 16 tile whose first two columns are 1, B = the layer's bias split
@@ -139,9 +135,9 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
   for (unsigned i = 0; i < kWaitLimit; ++i) {
     uint32_t done;
     asm volatile(
-        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(mbar), "r"(parity), "n"(kSuspendNs)
+        : "r"(mbar), "r"(parity)
         : "memory");
     if (done) return true;
   }

@@ -251,6 +251,22 @@ int check_device(const pcgb_fitter* ft) {
   return PCGB_OK;
 }
 
+// The LM constants in both precisions: an fp32-state kernel reads the float
+// copies instead of converting the doubles in every iteration (a double ->
+// float conversion issues on the FP64 pipe).
+void set_lm_constants(PcgbLmParams& p, double tol, double mu, double eta, double acc, double dec) {
+  p.tol = tol;
+  p.mu = mu;
+  p.eta = eta;
+  p.acc = acc;
+  p.dec = dec;
+  p.tol_f = float(tol);
+  p.mu_f = float(mu);
+  p.eta_f = float(eta);
+  p.acc_f = float(acc);
+  p.dec_f = float(dec);
+}
+
 int grid_for(int64_t n, int block) {
   int64_t g = (n + block - 1) / block;
   if (g < 1) g = 1;
@@ -676,11 +692,7 @@ int pcgb_multi_run(pcgb_multi* m, const pcgb_multi_job* jobs, int n_jobs, const 
     a.N = j.nprobs;
     a.n_items = j.nprobs;
     a.iters = iters;
-    a.tol = tol;
-    a.mu = mu;
-    a.eta = eta;
-    a.acc = acc;
-    a.dec = dec;
+    set_lm_constants(a, tol, mu, eta, acc, dec);
   }
   long long off = 0;
   for (int t = 0; t < n_jobs; ++t) {
@@ -771,11 +783,7 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
   prm.N = nprobs;
   prm.bstride = bounds_stride;
   prm.iters = iters;
-  prm.tol = tol;
-  prm.mu = mu;
-  prm.eta = eta;
-  prm.acc = acc;
-  prm.dec = dec;
+  set_lm_constants(prm, tol, mu, eta, acc, dec);
   const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_LM_C1_B1 : K_LM_C1_B0)
                                              : (bounds_stride == 0 ? K_LM_C0_B1 : K_LM_C0_B0);
   if (fb) {
@@ -1145,11 +1153,7 @@ int pcgb_random_search(pcgb_fitter* ft, const void* consts, int64_t consts_strid
   prm.iters = draws;
   prm.lm_iters = lm_iters;
   prm.seed = seed;
-  prm.tol = tol;
-  prm.mu = mu;
-  prm.eta = eta;
-  prm.acc = acc;
-  prm.dec = dec;
+  set_lm_constants(prm, tol, mu, eta, acc, dec);
   const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_RS_C1_B1 : K_RS_C1_B0)
                                              : (bounds_stride == 0 ? K_RS_C0_B1 : K_RS_C0_B0);
   return launch(ft, slot, prm, nprobs, 0, stream);
