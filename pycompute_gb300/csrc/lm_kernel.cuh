@@ -397,6 +397,9 @@ template <typename A> struct SameType<A, A> { static constexpr bool value = true
 // FP32 state with the FP64 solve / gain-ratio path above
 template <typename TA, typename TS>
 constexpr bool kMixed = SameType<TA, float>::value && SameType<TS, double>::value;
+// unroll factor of the per-sample loops of an iteration (see lm_iterate)
+template <typename TA, typename TS, int M>
+constexpr int sample_unroll() { return SameType<TA, float>::value && SameType<TS, float>::value ? M : 1; }
 
 // The iterations of one voxel on register state (lsqnonlin.py:823-924 per
 // iteration). cf(k, i) returns constant k of sample i; first receives the cost
@@ -415,11 +418,13 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
     for (int k = 0; k < P; ++k) g[k] = hd[k] = TA(0);
 #pragma unroll
     for (int k = 0; k < H; ++k) h[k] = TA(0);
-    // The sample loops stay rolled: unrolled over 16 samples the iteration no
-    // longer fits the instruction cache (measured on IVIM-16, 8.4 M voxels x 8
-    // iterations: 13.7 ms unrolled, 11.7 ms rolled; IVIM-10 x 20: 30.3 -> 28.3
-    // ms); the samples then sit in L1-cached local memory.
-#pragma unroll 1
+    // Sample loops: rolled where the FP64 pipe bounds the iteration (unrolled
+    // over 16 samples it no longer fits the instruction cache: IVIM-16, 8.4 M
+    // voxels x 8 iterations 13.7 ms unrolled, 11.7 ms rolled; IVIM-10 x 20:
+    // 30.3 -> 28.3 ms; the samples then sit in L1-cached local memory),
+    // unrolled where instruction issue bounds it (fp32 solve: IVIM-10, 1 M
+    // voxels x 20 iterations 1.21 ms unrolled, 1.45 ms rolled).
+#pragma unroll (sample_unroll<TA, TS, M>())
     for (int i = 0; i < M; ++i) {
       TA c[C > 0 ? C : 1];
 #pragma unroll
@@ -501,7 +506,7 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
 #pragma unroll
     for (int k = 0; k < P; ++k) pt[k] = p[k] - stp[k];
     TA ftp = TA(0);
-#pragma unroll 1
+#pragma unroll (sample_unroll<TA, TS, M>())
     for (int i = 0; i < M; ++i) {
       TA c[C > 0 ? C : 1];
 #pragma unroll
