@@ -334,7 +334,9 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
         mma_bf16(d_tmem, smem_desc(ones_s, 128, 256), smem_desc(bs, 128, 256), layer == 3 ? ID_OUT : ID_HID, 1u);
         mma_commit(mbar);
       }
-      const bool ok = mbar_wait(mbar, phase);
+      // one warp polls the mbarrier; the other three wait in the hardware
+      // barrier below and take no issue slots from the other tiles' epilogues
+      const bool ok = (warp & 3) != 0 || mbar_wait(mbar, phase);
       phase ^= 1u;
       if (wg_sync_any(g, !ok)) {
         lost = true;
