@@ -460,6 +460,13 @@ int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, int log_in, void*
                      const float* params, int nout, const int* kinds, const float* mean, const float* stdv,
                      float* targets, int64_t ldt, void* stream);
 
+/* The network's activation elementwise, for checks against other
+ * implementations: gelu_out[i] = gelu(z[i]) and grad_out[i] = gelu'(z[i]) as
+ * every network kernel computes them (GELU in bf16x2 arithmetic with
+ * tanh.approx.bf16x2; see the training and inference kernels). Either output
+ * may be NULL. No reference counterpart. */
+int pcgb_mlp_gelu(const float* z, int64_t n, float* gelu_out, float* grad_out, void* stream);
+
 /* Fused inference of all four layers: signals (nin, n) -> initial parameters
  * out (nout, n), clamped to [lb, ub]; log_in selects the input transform the
  * network was trained with. w_bf16 / w_master are host arrays of the

@@ -454,11 +454,30 @@ cudaError_t launch_gemm(int epi, const GemmArgs& g, dim3 grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
+// elementwise gelu(z) and gelu'(z) of the network's activation recipe
+__global__ void gelu_eval_kernel(const float* z, long long n, float* g, float* dg) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (g) g[i] = gelu(z[i]);
+  if (dg) dg[i] = gelu_grad(z[i]);
+}
+
 }  // namespace pcgb_mlp
 
 using namespace pcgb_mlp;
 
 extern "C" {
+
+int pcgb_mlp_gelu(const float* z, int64_t n, float* gelu_out, float* grad_out, void* stream) {
+  if (n < 0 || (n > 0 && !z)) return mlp_fail(PCGB_EINVAL, "bad gelu arguments");
+  if (n == 0) return PCGB_OK;
+  const long long blocks = (n + 255) / 256;
+  if (blocks > 0x7fffffffLL) return mlp_fail(PCGB_ERANGE, "gelu: n too large");
+  gelu_eval_kernel<<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(z, n, gelu_out, grad_out);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return mlp_fail(PCGB_ECUDA, cudaGetErrorString(e));
+  return PCGB_OK;
+}
 
 const char* pcgb_mlp_last_error(void) { return g_mlp_err.c_str(); }
 

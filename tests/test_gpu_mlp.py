@@ -6,12 +6,14 @@ relative, gradients to 1e-2 in relative Frobenius norm (a bf16 rounding of an
 activation that lands on the other side of a tie changes single entries by
 one bf16 ulp), fused inference to 1e-2 relative on the parameters.
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
 
 from oracle import mlp_oracle as mo
-from pycompute_gb300 import synth
+from pycompute_gb300 import _lib, synth
 from pycompute_gb300.warmstart import HID, WarmStartMLP
 
 pytestmark = pytest.mark.gpu
@@ -132,3 +134,32 @@ def test_training_reduces_loss_and_graph_matches_eager():
     np.testing.assert_allclose(g.losses, e.losses, rtol=0.05)
     for a, b in zip(g.layers, e.layers):
         torch.testing.assert_close(a.master, b.master, rtol=0.05, atol=2e-2)
+
+
+def test_gelu_recipe_matches_oracle():
+    """The activation every network kernel computes (2 gelu in bf16x2
+    arithmetic, tanh.approx.bf16x2) against the oracle's restatement of the
+    recipe: bit-equal except where the hardware tanh's truncated fp32
+    approximation and the truncated exact tanh fall on different bf16 values
+    (one ulp of t, so at most |z| ulp(t) / 2 in gelu); the derivative in fp32
+    to 1e-5 where t agrees."""
+    rng = np.random.default_rng(5)
+    z = np.concatenate([np.linspace(-12, 12, 240001), rng.standard_normal(100000) * 3,
+                        [0.0, -0.0, 1e-30, -1e-30, 40.0, -40.0]]).astype(np.float32)
+    zt = torch.from_numpy(z).to(DEV)
+    g = torch.empty_like(zt)
+    dg = torch.empty_like(zt)
+    rc = _lib.lib().pcgb_mlp_gelu(ctypes.c_void_p(zt.data_ptr()), zt.numel(), ctypes.c_void_p(g.data_ptr()),
+                                  ctypes.c_void_p(dg.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check("pcgb_mlp_gelu", rc)
+    torch.cuda.synchronize()
+    g, dg = g.cpu().numpy().astype(np.float64), dg.cpu().numpy().astype(np.float64)
+    want = mo.gelu(z)
+    same = g == want
+    assert same.mean() > 0.97, same.mean()
+    zb = mo.bf16(z)
+    assert np.all(np.abs(g - want) <= np.abs(zb) * 2.0 ** -9 + 1e-30), np.abs(g - want).max()
+    want_d = mo.gelu_grad(z.astype(np.float64))
+    ok = same & np.isfinite(want_d)
+    assert np.allclose(dg[ok], want_d[ok], rtol=1e-5, atol=1e-6)
+    assert g[np.where(z == 40.0)[0][0]] == 40.0 and g[np.where(z == -40.0)[0][0]] == 0.0

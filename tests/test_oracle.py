@@ -134,3 +134,30 @@ def test_gmw81_modifies_indefinite(ivim_oracle):
     x = om.gmw81_solve(np.array([[1.0], [2.0], [1.0]]), b[:, None])[:, 0]
     assert np.all(np.isfinite(x)) and x @ b > 0
     assert not np.allclose(A @ x, b)
+
+
+def test_bf16_rounding_helpers():
+    """bf16_exact rounds float64 values to bfloat16 in one step (ties to even)
+    and agrees with the float32 path on float32 inputs."""
+    from oracle import mlp_oracle as mo
+    rng = np.random.default_rng(3)
+    x = (rng.standard_normal(200000) * 10.0 ** rng.integers(-20, 20, 200000)).astype(np.float32).astype(np.float64)
+    assert np.array_equal(mo.bf16_exact(x), mo.bf16(x))
+    one, ulp = 1.0, 2.0 ** -7
+    ties = np.array([one + ulp / 2, one + 3 * ulp / 2, -(one + ulp / 2)])
+    assert np.array_equal(mo.bf16_exact(ties), [one, one + 2 * ulp, -one])
+    just_above = np.array([one + ulp / 2 + 2.0 ** -40])  # above the tie: a one-step rounding rounds up
+    assert mo.bf16_exact(just_above)[0] == one + ulp
+
+
+def test_gelu_oracle_recipe():
+    """The oracle's GELU follows the bf16 recipe: exact 0 at 0, the identity
+    for large z, 0 for very negative z, and a leak of z 2^-9 where the
+    truncated tanh stops one ulp short of -1."""
+    from oracle import mlp_oracle as mo
+    z = np.array([0.0, 10.0, -10.0, -4.0, 1.0])
+    g = mo.gelu(z)
+    assert g[0] == 0.0 and g[1] == 10.0 and g[2] == 0.0
+    assert g[3] == -4.0 * 2.0 ** -9
+    exact = 0.5 * z * (1 + np.tanh(np.sqrt(2 / np.pi) * (z + 0.044715 * z ** 3)))
+    assert abs(g[4] - exact[4]) < 4e-3
