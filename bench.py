@@ -76,6 +76,16 @@ TOL = 1e-4
 METRIC = "IVIM voxel fits/s at 1e-4 rel err vs FP64: MLP-warm-start vs plain LM, 1 GB300"
 # network FLOPs per voxel: 2 * (16*128 + 128*128 + 128*128 + 128*4)
 NET_FLOP_PER_VOXEL = 2 * (16 * 128 + 2 * 128 * 128 + 128 * 4)
+# Binding-unit work per unit, from the ncu opcode counts of the committed
+# profiles: FP64-pipe instructions (DFMA + DMUL + DADD) per IVIM voxel-iteration
+# of the FP64-solve LM (profiles/lm_fp64solve_ivim16_warm_4.2m.md) and MUFU
+# instructions per voxel of the tcgen05 network (profiles/mlp_infer_tc_ivim16_1m.md).
+FP64_OPS_PER_VOXEL_ITER = 82
+MUFU_PER_VOXEL_NET = 403
+# issue rates per SM per clock on sm_103a: FP64 at 1/64 of the 128 FP32 lanes,
+# MUFU 16 lanes
+FP64_PER_SM_CLK = 2
+MUFU_PER_SM_CLK = 16
 
 
 def _peaks():
@@ -300,6 +310,18 @@ def fp64_reference(w, data, iters=1000):
     solm.run(iters, tol=1e-30)
     torch.cuda.synchronize()
     return p
+
+
+def _unit_roofline(ops, ms, per_sm_clk, clocks, source):
+    """Achieved vs peak issue rate of one execution unit (instructions per
+    second over all SMs at the SM clock sampled under load)."""
+    import torch
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
+    peak = per_sm_clk * sms * mhz * 1e6
+    achieved = ops / (ms / 1e3)
+    return {"achieved": achieved, "peak": peak, "unit": "instructions/s", "frac": achieved / peak,
+            "work_source": source, "peak_source": f"{per_sm_clk} per SM per clock x {sms} SMs x {mhz:.0f} MHz"}
 
 
 def _stage_ms(events, a, b):
@@ -852,7 +874,14 @@ def main():
             "roofline_network": {"bound": "tensor", "achieved": net_tf, "peak": bf16_peak, "unit": "TFLOP/s",
                                  "frac": net_tf / bf16_peak, "kernel": "mlp_infer_tc_kernel (tcgen05)",
                                  "flop_per_voxel": NET_FLOP_PER_VOXEL, "kernel_ms": h["net_ms"],
-                                 "peak_source": peak_kind},
+                                 "peak_source": peak_kind,
+                                 "mufu": _unit_roofline(MUFU_PER_VOXEL_NET * N, h["net_ms"], MUFU_PER_SM_CLK,
+                                                        h["clocks"], "MUFU instructions per voxel, ncu opcode counts")},
+            "roofline_fp64": dict(_unit_roofline(FP64_OPS_PER_VOXEL_ITER * N * h["k_warm"], h["lm_ms"],
+                                                 FP64_PER_SM_CLK, h["clocks"],
+                                                 "FP64-pipe instructions (DFMA + DMUL + DADD) per voxel-iteration, "
+                                                 "ncu opcode counts"),
+                                  kernel="pcgb_lm (warm LM stage)", bound="fp64 pipe"),
             "warm_start": h["detail"],
             "plain_lm_ivim10_8.4M": ivim10,
             "mixed_batch": mixed,
