@@ -140,9 +140,10 @@ def test_gelu_recipe_matches_oracle():
     """The activation every network kernel computes (2 gelu in bf16x2
     arithmetic, tanh.approx.bf16x2) against the oracle's restatement of the
     recipe: bit-equal except where the hardware tanh's truncated fp32
-    approximation and the truncated exact tanh fall on different bf16 values
-    (one ulp of t, so at most |z| ulp(t) / 2 in gelu); the derivative in fp32
-    to 1e-5 where t agrees."""
+    approximation and the truncated exact tanh fall on different bf16 values.
+    One ulp of t (at most 2^-8) moves z t by |z| 2^-8, which can tip the bf16
+    rounding of z t + z by one ulp of the result (up to 2 |z| 2^-8): at most
+    1.5 |z| 2^-8 in gelu. The derivative in fp32 to 1e-5 where t agrees."""
     rng = np.random.default_rng(5)
     z = np.concatenate([np.linspace(-12, 12, 240001), rng.standard_normal(100000) * 3,
                         [0.0, -0.0, 1e-30, -1e-30, 40.0, -40.0]]).astype(np.float32)
@@ -158,7 +159,7 @@ def test_gelu_recipe_matches_oracle():
     same = g == want
     assert same.mean() > 0.97, same.mean()
     zb = mo.bf16(z)
-    assert np.all(np.abs(g - want) <= np.abs(zb) * 2.0 ** -9 + 1e-30), np.abs(g - want).max()
+    assert np.all(np.abs(g - want) <= np.abs(zb) * 1.5 * 2.0 ** -8 + 1e-30), np.abs(g - want).max()
     want_d = mo.gelu_grad(z.astype(np.float64))
     ok = same & np.isfinite(want_d)
     assert np.allclose(dg[ok], want_d[ok], rtol=1e-5, atol=1e-6)
