@@ -143,7 +143,9 @@ def test_gelu_recipe_matches_oracle():
     approximation and the truncated exact tanh fall on different bf16 values.
     One ulp of t (at most 2^-8) moves z t by |z| 2^-8, which can tip the bf16
     rounding of z t + z by one ulp of the result (up to 2 |z| 2^-8): at most
-    1.5 |z| 2^-8 in gelu. The derivative in fp32 to 1e-5 where t agrees."""
+    1.5 |z| 2^-8 in gelu. The derivative (fp32 on the GPU) agrees to 1e-5 for
+    most inputs and everywhere within what one ulp of t (at most |t| 2^-7)
+    moves it: (1/2 + |z t| k(z)) |t| 2^-7, k(z) = sqrt(2/pi) (1 + 3 0.044715 z^2)."""
     rng = np.random.default_rng(5)
     z = np.concatenate([np.linspace(-12, 12, 240001), rng.standard_normal(100000) * 3,
                         [0.0, -0.0, 1e-30, -1e-30, 40.0, -40.0]]).astype(np.float32)
@@ -160,7 +162,12 @@ def test_gelu_recipe_matches_oracle():
     assert same.mean() > 0.97, same.mean()
     zb = mo.bf16(z)
     assert np.all(np.abs(g - want) <= np.abs(zb) * 1.5 * 2.0 ** -8 + 1e-30), np.abs(g - want).max()
-    want_d = mo.gelu_grad(z.astype(np.float64))
-    ok = same & np.isfinite(want_d)
-    assert np.allclose(dg[ok], want_d[ok], rtol=1e-5, atol=1e-6)
+    zd = z.astype(np.float64)
+    want_d = mo.gelu_grad(zd)
+    _, t = mo._tanh_bf16(z)
+    k = np.sqrt(2 / np.pi) * (1 + 3 * 0.044715 * zd * zd)
+    tol = (0.5 + np.abs(zd * t) * k) * np.maximum(np.abs(t), 2.0 ** -126) * 2.0 ** -7 + 1e-6 + 1e-5 * np.abs(want_d)
+    assert np.all(np.isfinite(want_d))
+    assert np.isclose(dg, want_d, rtol=1e-5, atol=1e-6).mean() > 0.95
+    assert np.all(np.abs(dg - want_d) <= tol), np.max(np.abs(dg - want_d) / tol)
     assert g[np.where(z == 40.0)[0][0]] == 40.0 and g[np.where(z == -40.0)[0][0]] == 0.0
