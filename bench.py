@@ -149,8 +149,8 @@ class ClockSampler:
                     reasons.add(n)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        return {"sm_mhz": statistics.median(sm), "sm_mhz_min": min(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def _dist():
@@ -454,10 +454,11 @@ def warm_headline(args, ws, rank, local, dev):
     if ws > 1:
         dist.barrier()
     e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e_start.record(stream)
-    e2e_steps(args.steps)
-    e_end.record(stream)
-    torch.cuda.synchronize()
+    with ClockSampler(local) as e2e_clk:
+        e_start.record(stream)
+        e2e_steps(args.steps)
+        e_end.record(stream)
+        torch.cuda.synchronize()
     e2e_ms = max_over_ranks([e_start.elapsed_time(e_end) / args.steps], device=dev)[0]
     e2e_same = bool(torch.equal(outs[(args.steps - 1) % 2], warm_pars_h))
     # one volume on its own, streamed in chunks (WarmStartFitter.fit_host)
@@ -474,7 +475,8 @@ def warm_headline(args, ws, rank, local, dev):
     return {
         "N": N, "step_ms": step_ms, "plain_ms": plain_ms, "e2e_ms": e2e_ms, "lm_ms": lm_ms, "net_ms": net_ms,
         "e2e_single_ms": e2e_single_ms,
-        "stages": stages, "clocks": clk.summary(), "h2d": data_h.nbytes, "d2h": outs[0].nbytes,
+        "stages": stages, "clocks": clk.summary(), "e2e_clocks": e2e_clk.summary(), "h2d": data_h.nbytes,
+        "d2h": outs[0].nbytes,
         "k_warm": k_warm, "k_plain": k_plain, "e2e_same": e2e_same, "e2e_chunks": args.e2e_chunks,
         "detail": {
             "train_voxels": args.warm_train, "epochs": args.warm_epochs, "lr": args.warm_lr, "train_s": round(train_s, 3),
@@ -863,7 +865,7 @@ def main():
                     "d2h_bytes_per_step": h["d2h"], "ms_per_step": h["e2e_ms"],
                     "api": "WarmStartFitter.fit_stream: the timed steps as a sequence of pinned host volumes, "
                            "each copied in and back, copies overlapped with the neighbouring steps' fits",
-                    "matches_device_run": h["e2e_same"],
+                    "matches_device_run": h["e2e_same"], "clocks": h["e2e_clocks"],
                     "single_volume": {"value": ws * N / (h["e2e_single_ms"] / 1e3), "ms_per_step": h["e2e_single_ms"],
                                       "api": f"WarmStartFitter.fit_host, {h['e2e_chunks']} chunks"}},
             "roofline": {"bound": "hbm", "achieved": lm_gbs, "peak": hbm, "unit": "GB/s", "frac": lm_gbs / hbm,
