@@ -609,9 +609,18 @@ template <typename TA, int M, int NC> struct RegConsts {
   PCGB_HD TA operator()(int k, int i) const { return cv[k * M + i]; }
 };
 
-// All iterations of one voxel.
-template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
-PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
+// No epilogue after a voxel's fit.
+struct NoEpilogue {
+  template <class PArr, class DArr>
+  PCGB_HD void operator()(const PArr&, const DArr&) const {}
+  static constexpr bool kActive = false;
+};
+
+// All iterations of one voxel; then epi(p, d) with the final parameters and
+// the samples still in registers (a voxel converged before the call loads
+// them for the epilogue).
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B, class Epi = NoEpilogue>
+PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = Epi{}) {
   constexpr int P = Model::P, H = Model::H, C = Model::C;
   const long long N = a.N;
   if (a.step_type[v] == 0) {
@@ -621,6 +630,14 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
       const TA f0 = load<TA>(a.f, v);
       static_cast<TA*>(a.first_f)[v] = f0;
       static_cast<TA*>(a.last_f)[v] = f0;
+    }
+    if constexpr (Epi::kActive) {
+      TA p[P], d[M];
+#pragma unroll
+      for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * N + v);
+#pragma unroll
+      for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
+      epi(p, d);
     }
     return;
   }
@@ -671,6 +688,7 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v) {
     static_cast<TA*>(a.last_f)[v] = f;
   }
   if (a.iters_done) a.iters_done[v] += done;
+  if constexpr (Epi::kActive) epi(p, d);
 }
 
 // ---- refill schedule -----------------------------------------------------------
@@ -1100,20 +1118,24 @@ __device__ void warm_select_grid(const PcgbLmParams& a) {
 
 // The refit of the flagged voxels with the select as its epilogue
 // (grid-stride over the compacted list, count from a.n_items_dev).
+// the select of a refitted voxel as lm_fit_voxel's epilogue
+template <class Model, int M, typename TA, bool SHARED_C>
+struct SelectEpilogue {
+  const PcgbLmParams& a;
+  long long i, v;
+  static constexpr bool kActive = true;
+  PCGB_HD void operator()(const TA (&p)[Model::P], const TA (&d)[M]) const {
+    warm_select_voxel<Model, M, TA, SHARED_C>(a, i, v, p, d);
+  }
+};
+
 template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
 __device__ void lm_select_grid(const PcgbLmParams& a) {
   const long long n = device_count(a);
   const long long T = (long long)gridDim.x * blockDim.x;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += T) {
     const long long v = a.vox_idx[i];
-    VoxelFit<Model, M, TA, TS, SHARED_C, SHARED_B> s;
-    if (s.load(a, v)) {
-      while (!s.finished(a)) s.step(a);
-      s.store(a, v);
-    } else {
-      s.load_fit(a, v);
-    }
-    warm_select_voxel<Model, M, TA, SHARED_C>(a, i, v, s.p, s.d);
+    lm_fit_voxel<Model, M, TA, TS, SHARED_C, SHARED_B>(a, v, SelectEpilogue<Model, M, TA, SHARED_C>{a, i, v});
   }
 }
 

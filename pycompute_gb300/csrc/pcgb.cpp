@@ -77,8 +77,8 @@ constexpr int kMaxBlock = 256;
 struct pcgb_fitter {
   int P = 0, C = 0, M = 0, dtype = 0, sdtype = 0;
   int device = -1;
-  cudaLibrary_t lib[3] = {};  // one per kernel group, loaded on first use
-  int lm_min_blocks[3] = {};  // occupancy hint the group's LM kernels were built with (0: none)
+  cudaLibrary_t lib[4] = {};  // one per kernel group, loaded on first use
+  int lm_min_blocks[4] = {};  // occupancy hint the group's LM kernels were built with (0: none)
   cudaKernel_t k[K_COUNT] = {};
   std::string source, structname, cache_dir;
   std::mutex mu;
@@ -89,16 +89,21 @@ namespace {
 
 // Kernel groups, each its own NVRTC program, compiled when a kernel of the
 // group is first needed: 0 the fit itself (LM, cost, model evaluation, GMW81
-// solve), 1 the searches, 2 the refill schedule and the warm-start fallback.
-constexpr int kGroups = 3;
+// solve), 1 the searches, 2 the refill schedule and the warm-start fallback
+// check (also as the LM's epilogue), 3 the fallback refit with the select as
+// its epilogue. A group's LM kernels share one register cap (dropped when one
+// of them would spill too much), so the refit sits apart from the kernels
+// whose larger state cannot take the cap.
+constexpr int kGroups = 4;
 int group_of(int slot) {
   switch (slot) {
     case K_SEARCH_C1: case K_SEARCH_C0: case K_RS_C1_B1: case K_RS_C1_B0: case K_RS_C0_B1: case K_RS_C0_B0:
       return 1;
     case K_LMQ_C1_B1: case K_LMQ_C1_B0: case K_LMQ_C0_B1: case K_LMQ_C0_B0: case K_CHECK_C1: case K_CHECK_C0:
     case K_SELECT_C1: case K_SELECT_C0: case K_LMC_C1_B1: case K_LMC_C1_B0: case K_LMC_C0_B1: case K_LMC_C0_B0:
-    case K_LMS_C1_B1: case K_LMS_C1_B0: case K_LMS_C0_B1: case K_LMS_C0_B0:
       return 2;
+    case K_LMS_C1_B1: case K_LMS_C1_B0: case K_LMS_C0_B1: case K_LMS_C0_B0:
+      return 3;
     default:
       return 0;
   }
@@ -136,7 +141,7 @@ std::string program_source(const char* model_source, const char* model_struct, i
   const std::string lmb = lm_min_blocks > 0 ? "__launch_bounds__(" + std::to_string(kLmMaxThreads) + ", " +
                                                   std::to_string(lm_min_blocks) + ")"
                                             : std::string(bounds);
-  const bool g0 = group == 0, g1 = group == 1, g2 = group == 2;
+  const bool g0 = group == 0, g1 = group == 1, g2 = group == 2, g3 = group == 3;
   for (int c = 1; c >= 0 && g0; --c)
     for (int b = 1; b >= 0; --b)
       s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lm_c" << c << "_b" << b
@@ -155,14 +160,15 @@ std::string program_source(const char* model_source, const char* model_struct, i
         << "(const PcgbLmParams a) { pcgb::lm_refill_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
   for (int c = 1; c >= 0 && g2; --c)
-    for (int b = 1; b >= 0; --b) {
+    for (int b = 1; b >= 0; --b)
       s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lmc_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_check_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
+  for (int c = 1; c >= 0 && g3; --c)
+    for (int b = 1; b >= 0; --b)
       s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lms_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_select_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
-    }
   for (int c = 1; c >= 0 && g1; --c)
     s << "extern \"C\" __global__ void " << bounds << " pcgb_search_c" << c
       << "(const PcgbLmParams a) { pcgb::search_step_grid<PcgbModel, " << M << ", " << ta << ", "
