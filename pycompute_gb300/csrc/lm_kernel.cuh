@@ -4,12 +4,15 @@
 // launch parameters of lm_params.h.
 //
 // One thread owns one voxel for the whole fit: parameters, damping, the
-// packed normal matrix, the data samples and the bounds live in registers;
-// P, H = P(P+1)/2 and the sample count M are compile-time constants, so every
-// loop below unrolls and no array touches local memory. A voxel runs all of
-// its iterations inside one launch and leaves as soon as it converges (the
-// reference relaunches the kernel `iters` times and re-reads its state from
-// global memory each time, pycompute/cuda/lsqnonlin.py:1058-1068).
+// packed normal matrix, the solve and the bounds live in registers; P,
+// H = P(P+1)/2 and the sample count M are compile-time constants. The loops
+// over parameters unroll; the two loops over samples unroll only where
+// instruction issue bounds the iteration (fp32 solve) and stay rolled where
+// the FP64 pipe does (there the samples sit in L1-resident local memory; see
+// sample_unroll). A voxel runs all of its iterations inside one launch and
+// leaves as soon as it converges (the reference relaunches the kernel `iters`
+// times and re-reads its state from global memory each time,
+// pycompute/cuda/lsqnonlin.py:1058-1068).
 //
 // Numerics follow the reference kernel (pycompute/cuda/lsqnonlin.py:823-924)
 // step for step, with two type parameters:
