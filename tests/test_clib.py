@@ -68,6 +68,29 @@ def test_nvrtc_compiles_ivim_for_sm103a_within_spill_cap():
             assert len(spills) >= 2 and spills[1] == 0, spills
 
 
+def test_ivim16_fit_and_refit_kernels_keep_the_register_cap(tmp_path):
+    """IVIM-16, fp32 state and FP64 solve (the warm-start workload): the fit
+    kernel and the fallback refit + select kernel are both kept at the
+    6-blocks-per-SM register cap (80 registers). The refit shares no program
+    with the check-epilogue and refill kernels, which spill past the cap and
+    have their own group rebuilt without it."""
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    gm = codegen.generate(w.expr, w.pars, w.consts)
+    L = _lib.lib()
+    buf = ctypes.create_string_buffer(1 << 21)
+    rc = L.pcgb_fitter_compile(gm.source.encode(), gm.struct_name.encode(), gm.P, gm.C, w.M, 0, 1,
+                               str(tmp_path).encode(), buf, len(buf))
+    assert rc == 0, L.pcgb_last_error().decode()
+    log = buf.value.decode()
+
+    def registers(kernel):  # of the build the runtime loads: the last one in the log
+        block = log.split(f"Function properties for {kernel}\n")[-1]
+        return int(re.search(r"Used (\d+) registers", block).group(1))
+
+    assert registers("pcgb_lm_c1_b1") <= 80
+    assert registers("pcgb_lms_c1_b1") <= 80
+
+
 def test_compile_errors_are_reported():
     rc, _, err = _compile(codegen.GeneratedModel(expr="x", pars=["a"], consts=[], struct_name="Nope",
                                                  source="struct Nope { this is not C++ };", jnz=[True],
