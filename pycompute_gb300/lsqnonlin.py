@@ -26,7 +26,6 @@ Differences from the reference, all deliberate:
 from __future__ import annotations
 
 import ctypes
-import math
 from typing import Optional
 
 import torch

@@ -18,9 +18,7 @@ Every step is a kernel of libpcgb.so; PyTorch only holds the buffers.
 from __future__ import annotations
 
 import ctypes
-import math
 
-import numpy as np
 import torch
 
 from . import _lib

@@ -2,7 +2,6 @@
 IVIM (4, 10) and bi-exponential T2 (5, 32) fitted in one launch agree with
 the single-model fitter voxel by voxel; a captured CUDA graph replays the same
 fit; the autotuner returns a cached configuration."""
-import numpy as np
 import pytest
 import torch
 

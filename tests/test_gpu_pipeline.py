@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 import torch
 
-from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, codegen, parity, pipeline, synth
+from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, parity, pipeline, synth
 from pycompute_gb300.warmstart import WarmStartMLP
 
 pytestmark = pytest.mark.gpu
