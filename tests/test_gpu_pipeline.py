@@ -113,6 +113,49 @@ def test_fused_fallback_matches_separate_kernels(per_voxel_bounds, schedule, mod
     np.testing.assert_array_equal(c0, c1)
 
 
+def test_fallback_flags_match_the_rule_on_the_oracle():
+    """The fused check's flagged set against the fallback rule evaluated on the
+    CPU by the oracle, on the same warm fits: a voxel is flagged when its cost
+    is not finite or not below the cost at the plain fitter's constant start,
+    or a parameter is not strictly inside its bounds. GPU and oracle costs
+    differ by fp32 rounding, so the two sets may differ only on voxels whose
+    two costs are within 1e-5 relative of each other."""
+    from oracle import OracleModel
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    _, data = pipeline.synth_gpu(w, 50001, seed=9, device=DEV)
+    N = data.shape[1]
+    wf = pipeline.WarmStartFitter(w, _BadNet(w))
+    pars = wf.net.infer(data)
+    solm = wf._fitter()
+    prot, lb, ub = wf._consts(DEV)
+    solm.setup(pars, prot, data, lb, ub)
+    solm.lam_t.fill_(3e-3)
+    solm.run(2)
+    warm = pars.cpu().numpy().copy()
+    b = wf._buffers(w.P, N, DEV)
+    wf._warm_check(solm, data, pars, b)
+    torch.cuda.synchronize()
+    n_fb = int(b["counts"][0].item())
+    flagged_gpu = np.zeros(N, dtype=bool)
+    flagged_gpu[b["idx"][:n_fb].cpu().numpy()] = True
+
+    d = data.cpu().numpy()
+    om = OracleModel(w.expr, w.pars, w.consts)
+    consts = np.asarray(w.protocol, dtype=np.float32)
+    c = om.cost(warm, consts, d)
+    p0 = pipeline.init_constant(data, w.init_values).cpu().numpy()
+    c0 = om.cost(p0, consts, d)
+    lo = np.asarray(w.lb, dtype=np.float32)[:, None]
+    hi = np.asarray(w.ub, dtype=np.float32)[:, None]
+    on_bound = np.any(~((warm > lo) & (warm < hi)), axis=0)
+    with np.errstate(invalid="ignore"):
+        flagged_cpu = ~np.isfinite(c) | ~(c < c0) | on_bound
+        near_tie = np.abs(c.astype(np.float64) - c0) <= 1e-5 * np.maximum(np.abs(c0), 1e-30)
+    differ = flagged_gpu != flagged_cpu
+    assert n_fb > 0 and flagged_cpu.any()
+    assert np.all(near_tie[differ]), np.where(differ & ~near_tie)[0][:10]
+
+
 @pytest.mark.parametrize("N,chunks", [(100003, 3), (65536, 8), (1000, 4)])
 def test_fit_host_streams_chunks_with_fit_results(N, chunks):
     """fit_host (chunked copies overlapping the fits) gives every voxel the
