@@ -2,12 +2,12 @@
 
 Runs the reference's generated LM kernel
 ``test/ivim/second_order_levenberg_marquardt_4_1_21_f_f7def86f0a03.cu`` (built
-as host C++ into oracle/_ref by oracle/Makefile; the 10-sample build rewrites
-only its sample count) on seeded synthetic IVIM inputs and stores inputs and
+as host C++ into oracle/_ref by oracle/Makefile; the 10- and 16-sample builds
+rewrite only its sample count) on seeded synthetic IVIM inputs and stores inputs and
 outputs as small .npz files:
 
-  ivim{21,10}_it1.npz    one iteration (every quantity deterministic to ~1 ulp)
-  ivim{21,10}_it100.npz  100 iterations (the benchmark iteration count)
+  ivim{21,10,16}_it1.npz    one iteration (every quantity deterministic to ~1 ulp)
+  ivim{21,10,16}_it100.npz  100 iterations (the benchmark iteration count)
   ivim21_search.npz      one SearchStep launch of the random-search kernel
 
 Needs the reference tree (so only runs where it is mounted):
@@ -34,7 +34,7 @@ SEED = 20240611
 def main():
     if not build_reference():
         raise SystemExit("reference tree not found; fixtures are generated where it is mounted")
-    for M, bvals in ((21, synth.IVIM_B21), (10, synth.IVIM_B10)):
+    for M, bvals in ((21, synth.IVIM_B21), (10, synth.IVIM_B10), (16, synth.ivim_b16())):
         w = synth.ivim(bvals, name=f"ivim{M}")
         true, data, init, lb, ub, prot = w.generate(N, seed=SEED + M)
         ref = RefIVIM(M)

@@ -103,11 +103,17 @@ def assert_within_floor(oracles, w, out, init, prot, data, lb, ub, iters, solve_
     return o1, msg
 
 
-@pytest.mark.parametrize("M", [21, 10])
+def _ivim(M):
+    if M == 16:
+        return synth.ivim(synth.ivim_b16(), name="ivim16")
+    return synth.ivim(synth.IVIM_B21 if M == 21 else synth.IVIM_B10)
+
+
+@pytest.mark.parametrize("M", [21, 10, 16])
 @pytest.mark.parametrize("solve", [torch.float32, torch.float64])
 def test_one_iteration_matches_reference_golden(M, solve):
     g = _gold(f"ivim{M}_it1.npz")
-    w = synth.ivim(synth.IVIM_B21 if M == 21 else synth.IVIM_B10)
+    w = _ivim(M)
     out, _ = fit_gpu(w, g["data"], g["init"], g["lb"], g["ub"], g["protocol"], 1, solve_dtype=solve)
     np.testing.assert_array_equal(out["step_type"], g["step_type"])
     assert parity.compare_params(out["pars"], g["pars"])["max_rel"] < 1e-5
@@ -116,10 +122,10 @@ def test_one_iteration_matches_reference_golden(M, solve):
     assert np.all(out["iters"] == 1)
 
 
-@pytest.mark.parametrize("M", [21, 10])
+@pytest.mark.parametrize("M", [21, 10, 16])
 def test_full_fit_matches_reference_golden(M, oracles):
     g = _gold(f"ivim{M}_it100.npz")
-    w = synth.ivim(synth.IVIM_B21 if M == 21 else synth.IVIM_B10)
+    w = _ivim(M)
     # noise floor: the fp32 restatement on the CPU against the same golden run
     p_cpu = g["init"].copy()
     oracles(w).lm_run(p_cpu, g["protocol"], g["data"], g["lb"], g["ub"], 100)

@@ -32,7 +32,7 @@ def ivim_oracle():
     return OracleModel(synth.IVIM_EXPR, synth.IVIM_PARS, ["b"])
 
 
-@pytest.mark.parametrize("M", [21, 10])
+@pytest.mark.parametrize("M", [21, 10, 16])
 def test_oracle_one_iteration_matches_reference_golden(ivim_oracle, M):
     g = _gold(f"ivim{M}_it1.npz")
     p = g["init"].copy()
@@ -45,7 +45,7 @@ def test_oracle_one_iteration_matches_reference_golden(ivim_oracle, M):
     np.testing.assert_allclose(out["step"], g["step"], rtol=1e-3, atol=1e-6 * np.abs(g["step"]).max())
 
 
-@pytest.mark.parametrize("M", [21, 10])
+@pytest.mark.parametrize("M", [21, 10, 16])
 def test_oracle_100_iterations_matches_reference_golden(ivim_oracle, M):
     g = _gold(f"ivim{M}_it100.npz")
     p = g["init"].copy()
