@@ -115,3 +115,11 @@ def test_run_rejects_null_fitter():
                        None, None, None, 10, 10, None, 0, None, None, 0, None)
     assert rc == -22 and b"NULL" in L.pcgb_last_error()
     assert L.pcgb_fitter_destroy(None) == 0
+
+
+def test_elementwise_gelu_rejects_bad_arguments_without_a_gpu():
+    L = _lib.lib()
+    assert L.pcgb_mlp_gelu(None, 0, None, None, None) == 0
+    assert L.pcgb_mlp_gelu(None, 5, None, None, None) == -22
+    assert L.pcgb_mlp_last_error()
+    assert L.pcgb_mlp_gelu(None, -1, None, None, None) == -22
