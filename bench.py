@@ -889,7 +889,10 @@ def main():
             "mixed_batch": mixed,
             "precision_stress": stress,
             "cpu_baseline": cpu,
-            "gpu_launches": 5 * args.steps,
+            # our kernels per warm-start step: tcgen05 network, warm LM, fallback
+            # check, refit with select epilogue (the launch list of the timed steps
+            # in profiles/launches_warm_step_ivim16_16.7M.md; the state fills are PyTorch's)
+            "gpu_launches": 4 * args.steps,
             "clocks": h["clocks"],
         }
         print(json.dumps(line), flush=True)
