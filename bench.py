@@ -76,10 +76,11 @@ TOL = 1e-4
 METRIC = "IVIM voxel fits/s at 1e-4 rel err vs FP64: MLP-warm-start vs plain LM, 1 GB300"
 # network FLOPs per voxel: 2 * (16*128 + 128*128 + 128*128 + 128*4)
 NET_FLOP_PER_VOXEL = 2 * (16 * 128 + 2 * 128 * 128 + 128 * 4)
-# Binding-unit work per unit, from the ncu opcode counts of the committed
-# profiles: FP64-pipe instructions (DFMA + DMUL + DADD) per IVIM voxel-iteration
-# of the FP64-solve LM (profiles/lm_fp64solve_ivim16_warm_4.2m.md) and MUFU
-# instructions per voxel of the tcgen05 network (profiles/mlp_infer_tc_ivim16_1m.md).
+# Binding-unit work per unit, from ncu opcode counts (sass__inst_executed per
+# opcode over one launch, divided by the units it processed): FP64-pipe
+# instructions (56 DFMA + 24 DMUL + 2 DADD) per IVIM-16 voxel-iteration of the
+# FP64-solve LM (4,194,304 warm-started voxels x 2 iterations) and MUFU
+# instructions per voxel of the tcgen05 network (1,048,576 IVIM-16 voxels).
 FP64_OPS_PER_VOXEL_ITER = 82
 MUFU_PER_VOXEL_NET = 403
 # issue rates per SM per clock on sm_103a: FP64 at 1/64 of the 128 FP32 lanes,
@@ -170,13 +171,18 @@ def _median_rel_np(a, b):
     return float(np.median(r)), float(np.mean(r > TOL))
 
 
-def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 30, plan: dict | None = None):
+_CPU_INPUTS = {}  # the timed sample's host inputs, kept for the repeated timings
+
+
+def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 30, plan: dict | None = None,
+                         n_fixed: int | None = None):
     """The reference algorithm (plain LM, fp32) on the host cores, on IVIM-16
     at the smallest iteration budget whose median error against the all-FP64
     CPU fit (same LM, constant start, 300 iterations) is <= 1e-4. The sample
-    grows until one fit takes at least target_s / 4; that size is timed once.
-    With ``plan`` (the result of an earlier call) the budget and the sample
-    size are reused and only the timed fit runs again.
+    grows until one fit takes at least target_s / 4 (or is ``n_fixed`` voxels);
+    that size is timed once. With ``plan`` (the result of an earlier call) the
+    budget and the sample size are reused and only the timed fit runs again
+    (on the inputs made by the first call).
     """
     from oracle import OracleModel, RefIVIM, ref_available
     from pycompute_gb300 import synth
@@ -190,8 +196,8 @@ def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 3
     else:
         impl, kind = port, "port"
     if plan is not None:
-        k_run, curve, n = plan["iters"], plan["curve"], plan["n"]
-        _, data, init, lb, ub, prot = w.generate(n, seed=8)
+        k_run, n = plan["iters"], plan["n"]
+        data, init, lb, ub, prot = _CPU_INPUTS[n]
         p = init.copy()
         t0 = time.perf_counter()
         impl.lm_run(p, prot, data, lb, ub, k_run)
@@ -210,16 +216,18 @@ def cpu_reference_at_tol(target_s: float, n_ref: int = 16384, max_iters: int = 3
             k_tol = k
             break
     k_run = k_tol if k_tol is not None else max_iters
-    n = 1 << 16
+    n = n_fixed or (1 << 16)
     while True:
         _, data, init, lb, ub, prot = w.generate(n, seed=8)
         p = init.copy()
         t0 = time.perf_counter()
         impl.lm_run(p, prot, data, lb, ub, k_run)
         el = time.perf_counter() - t0
-        if el >= target_s / 4 or n >= (1 << 23):
+        if n_fixed or el >= target_s / 4 or n >= (1 << 23):
             break
         n *= 2 if el > 0.05 else 8
+    _CPU_INPUTS.clear()
+    _CPU_INPUTS[n] = (data, init, lb, ub, prot)
     what = "reference generated kernel" if kind == "reference" else "fp32 oracle port"
     sample = (f"{n} IVIM-16 voxels x {k_run} iterations (the 1e-4 budget on {n_ref} voxels vs the all-FP64 CPU fit; "
               f"{what}, {cores} threads), {el:.2f} s")
@@ -700,36 +708,63 @@ def precision_stress(n=1 << 21, iters=100, seed=400):
     return out
 
 
-def _config(args, ws, k_warm=None, k_plain=None):
+def _config(args, ws):
+    """The workload, identical in both arms (iteration budgets are results and
+    travel outside it)."""
     return {"workload": "ivim16_warm_start_vs_plain_lm_16.7M", "voxels_per_gpu": args.warm_voxels,
-            "ndata": M_IVIM16, "nparam": P_IVIM, "tolerance": TOL, "iters_warm": k_warm, "iters_plain": k_plain,
+            "ndata": M_IVIM16, "nparam": P_IVIM, "tolerance": TOL,
             "network": "16-128-128-128-4 GELU, bf16 weights, fp32 accumulate",
             "train_voxels": args.warm_train, "solve": "f64", "init_plain": "constant [max S, 0.1, 1e-2, 1e-3]",
             "l2": "inputs larger than L2 (1.07 GB signals per GPU)", "parallelism": f"voxel shards x{ws}"}
+
+
+def _torch_ivim_inputs(bvals, n, seed, dev):
+    """Seeded Rician IVIM signals (M, n) and the reference notebook's constant
+    start, made with PyTorch alone (the reference arm loads none of this
+    package's native code): true parameters uniform over the benchmark
+    ranges, sigma = S0 / 50."""
+    import torch
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    u = lambda lo, hi: lo + (hi - lo) * torch.rand(n, generator=g, device=dev, dtype=torch.float64)  # noqa: E731
+    s0, f, dstar, d = u(500.0, 1500.0), u(0.05, 0.35), u(5e-3, 5e-2), u(0.5e-3, 2.5e-3)
+    b = torch.tensor(bvals, device=dev, dtype=torch.float64)[:, None]
+    clean = s0 * (f * torch.exp(-b * dstar) + (1 - f) * torch.exp(-b * d))
+    sigma = s0 / 50.0
+    n1 = torch.randn(clean.shape, generator=g, device=dev, dtype=torch.float64)
+    n2 = torch.randn(clean.shape, generator=g, device=dev, dtype=torch.float64)
+    data = torch.sqrt((clean + sigma * n1) ** 2 + (sigma * n2) ** 2).float().contiguous()
+    del clean, n1, n2
+    init = torch.stack([data.amax(dim=0), torch.full((n,), 0.1, device=dev), torch.full((n,), 1e-2, device=dev),
+                        torch.full((n,), 1e-3, device=dev)]).contiguous()
+    return data, init
 
 
 def reference_gpu_kernel(steps: int = 3):
     """The reference's own LM kernel on this GPU, launched as its run() does
     (oracle/_ref cubin built from the reference tree; 32-thread blocks, one
     launch per iteration): IVIM-10 8,388,608 voxels x 100 iterations, and
-    IVIM-16 16,777,216 voxels at the plain LM's 1e-4 budget (8 iterations)."""
+    IVIM-16 16,777,216 voxels at the plain LM's 1e-4 budget (8 iterations).
+    Inputs are made with PyTorch alone: this process maps none of the
+    package's native libraries."""
     import torch
     from oracle import ref_gpu
-    from pycompute_gb300 import pipeline, synth
+    from pycompute_gb300 import synth
 
     out = {"kernel": "reference generated LM kernel (printf dropped, parameter loads bounded), sm_103a",
            "launch": "ceil(N/32) blocks x 32 threads, one launch per iteration, protocol tiled per voxel"}
-    for name, w, n, iters in (("ivim10_8.4M_100it", synth.ivim(), 256 * 256 * 128, 100),
-                              ("ivim16_16.7M_8it_at_1e-4", synth.ivim(synth.ivim_b16(), name="ivim16"), 1 << 24, 8)):
-        if not ref_gpu.available(w.M):
-            out[name] = {"unavailable": f"oracle/_ref cubin for {w.M} samples not built"}
+    dev = torch.device("cuda", torch.cuda.current_device())
+    for name, bvals, n, iters in (("ivim10_8.4M_100it", synth.IVIM_B10, 256 * 256 * 128, 100),
+                                  ("ivim16_16.7M_8it_at_1e-4", synth.ivim_b16(), 1 << 24, 8)):
+        M = len(bvals)
+        if not ref_gpu.available(M):
+            out[name] = {"unavailable": f"oracle/_ref cubin for {M} samples not built"}
             continue
-        _, data = pipeline.synth_gpu(w, n, seed=1000, device="cuda")
-        init = pipeline.init_constant(data, w.init_values)
-        consts = torch.tensor(w.protocol, device="cuda")[:, None].expand(w.M, n).contiguous()
-        lb = torch.tensor(w.lb, device="cuda")[:, None].expand(4, n).contiguous()
-        ub = torch.tensor(w.ub, device="cuda")[:, None].expand(4, n).contiguous()
-        ref = ref_gpu.RefGpuIVIM(w.M)
+        data, init = _torch_ivim_inputs(bvals, n, 1000, dev)
+        consts = torch.tensor(bvals, device=dev, dtype=torch.float32)[:, None].expand(M, n).contiguous()
+        lb = torch.tensor(synth.IVIM_LB, device=dev)[:, None].expand(4, n).contiguous()
+        ub = torch.tensor(synth.IVIM_UB, device=dev)[:, None].expand(4, n).contiguous()
+        ref = ref_gpu.RefGpuIVIM(M)
         pars = init.clone()
 
         def step():
@@ -744,13 +779,23 @@ def reference_gpu_kernel(steps: int = 3):
     return out
 
 
+def _mapped_native_libraries():
+    """Shared objects of this repository mapped into this process (Linux)."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {line.split()[-1] for line in f if line.rstrip().endswith(".so") or ".so." in line}
+    except OSError:
+        return None
+    return sorted(os.path.relpath(p, ROOT) for p in paths if p.startswith(ROOT + os.sep))
+
+
 def run_reference_arm(args):
     ws, rank, local = _dist()
     if rank != 0:
         return 0
-    # the budget and the sample size are settled once; every step then times
-    # one bounded fit of the sample (about cpu_seconds / 4 of host time)
-    plan = cpu_reference_at_tol(target_s=args.cpu_seconds)
+    # the budget is settled once on a small sample; every step then times one
+    # host fit of the full workload (all voxels of a GPU's shard)
+    plan = cpu_reference_at_tol(target_s=args.cpu_seconds, n_fixed=args.warm_voxels)
     vals, last = [], plan
     for s in range(args.warmup + args.steps):
         last = cpu_reference_at_tol(target_s=args.cpu_seconds, plan=plan)
@@ -767,13 +812,17 @@ def run_reference_arm(args):
         gpu = {"unavailable": f"{type(e).__name__}: {e}"}
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "fits/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": args.warm_voxels / value * 1e3,
+        "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded IVIM-16, Rician SNR 50)",
-        "config": dict(_config(args, 1, None, last["iters"]), method="plain LM (the reference has no warm start)"),
+        "config": _config(args, ws),
+        "method": "plain LM from the constant start (the reference has no warm start)",
+        "iters_plain": last["iters"],
         "cpu_baseline": {"value": value, "unit": "fits/s", "cores": last["cores"], "kind": last["kind"],
                          "sample": last["sample"]},
         "e2e": {"value": value, "unit": "fits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_reference_kernel": gpu,
+        "native_libraries_mapped": _mapped_native_libraries(),
     }
     print(json.dumps(line), flush=True)
     return 0
@@ -858,7 +907,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": h["step_ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 state, f64 GMW81 solve + gain ratio, bf16 network",
             "data": "synthetic (seeded IVIM-16, Rician SNR 50; network trained on other seeded signals)",
-            "config": _config(args, ws, h["k_warm"], h["k_plain"]),
+            "config": _config(args, ws),
+            "iters_warm": h["k_warm"], "iters_plain": h["k_plain"],
             "plain_lm": {"value": plain_value, "unit": "fits/s", "ms_per_step": h["plain_ms"],
                          "iters": h["k_plain"], "speedup_warm_vs_plain": value / plain_value},
             "e2e": {"value": ws * N / (h["e2e_ms"] / 1e3), "unit": "fits/s", "h2d_bytes_per_step": h["h2d"],
@@ -890,8 +940,8 @@ def main():
             "precision_stress": stress,
             "cpu_baseline": cpu,
             # our kernels per warm-start step: tcgen05 network, warm LM, fallback
-            # check, refit with select epilogue (the launch list of the timed steps
-            # in profiles/launches_warm_step_ivim16_16.7M.md; the state fills are PyTorch's)
+            # check, refit with select epilogue (counted from an ncu launch list of
+            # the timed steps; the state fills are PyTorch's)
             "gpu_launches": 4 * args.steps,
             "clocks": h["clocks"],
         }

@@ -307,7 +307,10 @@ int pcgb_multi_grid(const pcgb_multi* program);
  * launch. order (host, may be NULL = program order) is the order in which the
  * work queue hands out the jobs' chunks (longest work first shortens the
  * tail). work_counter: one uint32 of device scratch, zeroed by this call
- * (cudaMemsetAsync) before the launch; grid <= 0 selects the persistent grid. */
+ * (cudaMemsetAsync) before the launch; grid <= 0 selects the persistent grid.
+ * At most 2^31 chunks of `chunk` voxels per call, summed over the jobs (the
+ * counter is 32 bits wide); larger requests fail with PCGB_ERANGE before any
+ * work is queued. */
 int pcgb_multi_run(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, const int* order, int iters,
                    double tol, double mu, double eta, double acc, double dec, int chunk, int grid,
                    uint32_t* work_counter, void* stream);
@@ -316,14 +319,14 @@ int pcgb_multi_run(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, 
  * pcgb_multi_run for callers that cannot allocate device memory. No reference
  * counterpart: the reference always allocates its buffers through CuPy.
  *
- * Who needs it: code that runs while a CUDA graph is being captured (a
- * cudaMalloc there breaks the capture), hosts whose device memory belongs to
- * another framework's pool allocator, and embedded callers that may not grow
- * device memory after start-up. pcgb_multi_run needs one word of device
- * scratch (the work counter); this variant uses a statically allocated
- * 256-byte array owned by the library instead, so it allocates nothing and
- * calls no allocating routine. The caller still passes every input and output
- * (the jobs' buffers).
+ * Who needs it: hosts whose device memory belongs to another framework's pool
+ * allocator (which hands out only the buffers it manages, so a side
+ * cudaMalloc would fragment or exceed its budget), and embedded or
+ * long-running services that reserve their device memory at start-up and may
+ * not grow it afterwards. pcgb_multi_run needs one word of device scratch (the
+ * work counter); this variant uses a statically allocated 256-byte array owned
+ * by the library instead, so it allocates nothing and calls no allocating
+ * routine. The caller still passes every input and output (the jobs' buffers).
  *
  * Limits and rules:
  *  - at most 2^31 chunks of `chunk` voxels per call (summed over the jobs);
@@ -335,8 +338,11 @@ int pcgb_multi_run(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, 
  *    the GPU (concurrent streams, or several host threads) race on it, so
  *    serialise them;
  *  - the first call on each device looks up the array's device address
- *    (cudaGetSymbolAddress, with that device current); make that first call
- *    before any stream capture.
+ *    (cudaGetSymbolAddress, with that device current) and caches it with the
+ *    identity of the current CUDA context; make that first call before any
+ *    stream capture. A later call under another context (after a
+ *    cudaDeviceReset, or with another driver-API context current) looks the
+ *    address up again, so it again must not come during a capture.
  */
 int pcgb_multi_run_noalloc(pcgb_multi* program, const pcgb_multi_job* jobs, int n_jobs, const int* order, int iters,
                            double tol, double mu, double eta, double acc, double dec, int chunk, int grid,

@@ -204,8 +204,8 @@ def ref_available(ndata: int = 21) -> bool:
     return os.path.exists(os.path.join(REF_DIR, f"libref_ivim{ndata}.so"))
 
 
-def build_reference(ref_root: str = "/root/reference") -> bool:
-    """Build oracle/_ref from the reference tree when it is present."""
+def build_reference(ref_root: str) -> bool:
+    """Build oracle/_ref from the reference tree at ref_root when it is present."""
     if not os.path.isdir(ref_root):
         return False
     r = subprocess.run(["make", "-s", "-C", HERE, f"REF={ref_root}"], capture_output=True, text=True)

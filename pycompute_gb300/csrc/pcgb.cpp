@@ -71,6 +71,8 @@ const char* kKernelNames[K_COUNT] = {"pcgb_lm_c1_b1", "pcgb_lm_c1_b0", "pcgb_lm_
 
 constexpr int kDefaultBlock = 128;
 constexpr int kMaxBlock = 256;
+// most chunks one mixed-model launch may hand out (see pcgb_multi_run)
+constexpr int64_t kMaxMultiChunks = int64_t(1) << 31;
 
 }  // namespace
 
@@ -648,10 +650,26 @@ int pcgb_multi_run(pcgb_multi* m, const pcgb_multi_job* jobs, int n_jobs, const 
                    double mu, double eta, double acc, double dec, int chunk, int grid, uint32_t* work_counter,
                    void* stream) {
   g_err.clear();
-  if (!m) return fail(PCGB_EINVAL, "program is NULL");
-  if (!jobs || n_jobs != m->n) return fail(PCGB_EINVAL, "need one job per model of the program (%d)", m->n);
-  if (iters < 0) return fail(PCGB_EINVAL, "iters must be >= 0");
+  if (!jobs || n_jobs < 1 || n_jobs > PCGB_MAX_MODELS) return fail(PCGB_EINVAL, "need 1..%d jobs", PCGB_MAX_MODELS);
   if (chunk < 32 || chunk % 32 || chunk > 4096) return fail(PCGB_EINVAL, "chunk must be a multiple of 32 up to 4096");
+  // The warps claim chunk indices from a 32-bit counter up to (chunks + warps
+  // of the grid); at most 2^31 chunks keep those claims below 2^32, so the
+  // counter cannot wrap and hand out a chunk twice. Checked before anything
+  // else touches the GPU, summing without overflow.
+  {
+    int64_t chunks = 0;
+    for (int k = 0; k < n_jobs; ++k) {
+      const int64_t n = jobs[k].nprobs;
+      if (n < 0) return fail(PCGB_EINVAL, "job %d: nprobs < 0", k);
+      chunks += n / chunk + (n % chunk != 0);
+      if (chunks > kMaxMultiChunks)
+        return fail(PCGB_ERANGE, "too many voxels for one call: at most 2^31 chunks of `chunk` voxels over all jobs "
+                                 "(use a larger chunk or split the call)");
+    }
+  }
+  if (!m) return fail(PCGB_EINVAL, "program is NULL");
+  if (n_jobs != m->n) return fail(PCGB_EINVAL, "need one job per model of the program (%d)", m->n);
+  if (iters < 0) return fail(PCGB_EINVAL, "iters must be >= 0");
   if (!work_counter) return fail(PCGB_EINVAL, "work_counter is NULL");
   int dev = -1;
   cudaGetDevice(&dev);

@@ -10,7 +10,8 @@ outputs as small .npz files:
   ivim{21,10,16}_it100.npz  100 iterations (the benchmark iteration count)
   ivim21_search.npz      one SearchStep launch of the random-search kernel
 
-Needs the reference tree (so only runs where it is mounted):
+Needs the reference tree (PCGB_REFERENCE_TREE, or a `reference` directory
+beside this repository):
     python tests/golden/make_golden.py
 """
 from __future__ import annotations
@@ -32,8 +33,11 @@ SEED = 20240611
 
 
 def main():
-    if not build_reference():
-        raise SystemExit("reference tree not found; fixtures are generated where it is mounted")
+    from __graft_entry__ import reference_tree
+
+    ref_root = reference_tree()
+    if not ref_root or not build_reference(ref_root):
+        raise SystemExit("reference tree not found (set PCGB_REFERENCE_TREE); fixtures are generated where it exists")
     for M, bvals in ((21, synth.IVIM_B21), (10, synth.IVIM_B10), (16, synth.ivim_b16())):
         w = synth.ivim(bvals, name=f"ivim{M}")
         true, data, init, lb, ub, prot = w.generate(N, seed=SEED + M)

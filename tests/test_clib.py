@@ -123,3 +123,30 @@ def test_elementwise_gelu_rejects_bad_arguments_without_a_gpu():
     assert L.pcgb_mlp_gelu(None, 5, None, None, None) == -22
     assert L.pcgb_mlp_last_error()
     assert L.pcgb_mlp_gelu(None, -1, None, None, None) == -22
+
+
+@pytest.mark.parametrize("entry", ["pcgb_multi_run", "pcgb_multi_run_noalloc"])
+def test_mixed_run_refuses_more_than_2_31_chunks_before_any_gpu_work(entry):
+    """Both mixed-model entry points refuse a request whose chunk count would
+    let the 32-bit work counter wrap (2^31 chunks over all jobs, summed without
+    overflow), before they look at the program or touch the GPU: here no
+    program and no GPU exist at all."""
+    from pycompute_gb300.multi import _Job
+
+    L = _lib.lib()
+    cases = [[(1 << 31) * 64 + 1], [1 << 62, 1 << 62], [(1 << 63) - 1, (1 << 63) - 1], [(1 << 30) * 64] * 3]
+    for sizes in cases:
+        arr = (_Job * len(sizes))()
+        for j, n in zip(arr, sizes):
+            j.nprobs = n
+        args = [None, arr, len(sizes), None, 1, 1e-8, 0.25, 0.75, 0.2, 2.0, 64, 0]
+        rc = getattr(L, entry)(*args, *([None] if entry == "pcgb_multi_run" else []), None)
+        assert rc == -34, (sizes, rc)
+        err = L.pcgb_noalloc_last_error() if entry.endswith("noalloc") else L.pcgb_last_error()
+        assert b"2^31" in err
+    # exactly 2^31 chunks passes the range check and fails on the missing program
+    arr = (_Job * 1)()
+    arr[0].nprobs = (1 << 31) * 64
+    rc = getattr(L, entry)(None, arr, 1, None, 1, 1e-8, 0.25, 0.75, 0.2, 2.0, 64, 0,
+                           *([None] if entry == "pcgb_multi_run" else []), None)
+    assert rc != -34

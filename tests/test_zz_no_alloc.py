@@ -1,16 +1,16 @@
 """The allocation-free mixed-model entry point, pcgb_multi_run_noalloc.
 
-It is for callers that cannot allocate device memory (a graph capture in
-progress, a host whose device memory belongs to another allocator, an
-embedded caller that may not grow its footprint): it keeps the work counter in
-a library-owned static device array instead of a caller-allocated word. Here
-it is called through the C ABI twice in a row and must give the same fit as
-pcgb_multi_run with a caller-provided counter, on every voxel. The file is
+It is for callers that cannot allocate device memory (a host whose device
+memory belongs to another framework's pool allocator, a service that reserves
+its memory at start-up and may not grow it): it keeps the work counter in a
+library-owned static device array instead of a caller-allocated word. Here it
+is called through the C ABI twice in a row and must give the same fit as
+pcgb_multi_run with a caller-provided counter, bit for bit on every voxel
+(a voxel's fit does not depend on which warp claims its chunk). The file is
 named so that pytest collects it last.
 """
 import ctypes
 
-import numpy as np
 import pytest
 import torch
 
@@ -50,17 +50,17 @@ def test_noalloc_matches_caller_scratch_twice_in_a_row():
     iters = 40
     fitter.fit(jobs, iters)  # caller-provided work counter
     torch.cuda.synchronize()
-    want = [(j.pars.clone(), j.step_type.clone(), j.f.clone()) for j in jobs]
+    want = [(j.pars.clone(), j.step_type.clone(), j.f.clone(), j.iters.clone()) for j in jobs]
     for _ in range(2):  # the shared counter must be cleared between calls
         _reset(jobs, inits)
         _noalloc(fitter, jobs, iters)
         torch.cuda.synchronize()
-        for (p, st, f), j in zip(want, jobs):
-            rel = ((j.pars.double() - p.double()).abs() / p.double().abs().clamp_min(1e-30)).max().item()
-            assert rel <= 1e-6, rel
+        for (p, st, f, it), j in zip(want, jobs):
+            assert torch.equal(j.pars, p)
             assert torch.equal(j.step_type, st)
+            assert torch.equal(j.f, f)
+            assert torch.equal(j.iters, it)
             assert torch.all(j.iters > 0)
-            np.testing.assert_allclose(j.f.cpu().numpy(), f.cpu().numpy(), rtol=1e-6)
 
 
 def test_noalloc_rejects_oversized_requests():
