@@ -135,8 +135,10 @@ def test_full_fit_matches_reference_golden(M, oracles):
         rep = parity.compare_params(out["pars"], g["pars"])
         assert rep["median_rel"] < 1e-5, rep
         assert rep["frac_gt_1e-4"] <= floor + 0.05, (rep, floor)
-        # ~0.3 % of IVIM voxels meet the fp32 convergence test; on 512 voxels a
-        # few flips are noise (the large-N tests hold 99.9 %)
+        # ~0.3 % of IVIM voxels meet the fp32 convergence test, a rounding-noise
+        # event at tol 1e-8; on 512 voxels a few flips are noise (the large-N
+        # tests hold the measured fp32-vs-fp32 floor, and the lockstep test in
+        # test_gpu_reference_kernel.py holds every fp32-resolved decision)
         assert parity.flags_agree(out["step_type"], g["step_type"]) >= 0.99
 
 

@@ -161,3 +161,24 @@ def test_gelu_oracle_recipe():
     assert g[3] == -4.0 * 2.0 ** -9
     exact = 0.5 * z * (1 + np.tanh(np.sqrt(2 / np.pi) * (z + 0.044715 * z ** 3)))
     assert abs(g[4] - exact[4]) < 4e-3
+
+
+@pytest.mark.skipif(not ref_available(10), reason="reference kernel not built (no reference tree)")
+def test_oracle_lockstep_with_reference_host_build():
+    """The fp32 oracle against the reference's own kernel built for the host,
+    in lockstep (both start every iteration of a 100-iteration IVIM-10 run from
+    the reference's state): no decision that fp32 resolves differs; the raw
+    step-code agreement over all voxels stays at the measured 96 % (the rest
+    are voxels at rest, decided by the two builds' rounding); parameters of the
+    resolved voxel-iterations agree to 1e-5 on 99.7 % (measured; the rest are
+    ill-conditioned voxels whose fp32 steps differ along a flat direction)."""
+    from oracle import RefIVIM
+    from oracle.lockstep import lockstep_host, summarise
+
+    w = synth.ivim()
+    _, data, init, lb, ub, prot = w.generate(8192, seed=31)
+    o = OracleModel(w.expr, w.pars, w.consts)
+    rep = summarise(lockstep_host(RefIVIM(10), o, init, prot, data, lb, ub, 100, solve_dtype=np.float32))
+    assert rep["mismatch_resolved_total"] == 0, rep
+    assert rep["min_same_step_code"] >= 0.95, rep
+    assert rep["params_within_1e-5_resolved"] >= 0.995, rep
