@@ -266,6 +266,87 @@ def cpu_parity_ivim10(n: int = 1 << 18, iters: int = 100):
     return out
 
 
+def parity_c2(n: int = 256 * 256 * 128, iters: int = 100):
+    """The checker at the plain-LM-at-scale size (IVIM-10, 8,388,608 voxels,
+    100 iterations): the fitter against the reference's own generated kernel
+    (oracle/_ref, built from the reference tree for sm_103a, launched as its
+    run() does) on the same voxels, both free-running and in lockstep, and
+    both against the all-FP64 fitter (same LM, same start, 100 iterations,
+    tol 1e-8). Not timed."""
+    import torch
+    from oracle import lockstep, ref_gpu
+    from pycompute_gb300 import Expr, SecondOrderLevenbergMarquardt, parity, pipeline, synth
+
+    w = synth.ivim()
+    if not ref_gpu.available(w.M):
+        return {"unavailable": "oracle/_ref cubin not built (no reference tree where build() ran)"}
+    dev = torch.device("cuda", torch.cuda.current_device())
+    _, data = pipeline.synth_gpu(w, n, seed=2024, device=dev)
+    init = pipeline.init_constant(data, w.init_values)
+    prot = torch.tensor(w.protocol, device=dev)
+    lb_t, ub_t = torch.tensor(w.lb, device=dev), torch.tensor(w.ub, device=dev)
+    tile = lambda v, k: v[:, None].expand(k, n).contiguous()  # noqa: E731
+
+    def reference(lockstep_with=None):
+        r = ref_gpu.RefGpuIVIM(w.M)
+        p = init.clone()
+        r.setup(p, tile(prot, w.M), data, tile(lb_t, 4), tile(ub_t, 4))
+        if lockstep_with is None:
+            r.run(iters)
+            torch.cuda.synchronize()
+            return r, None
+        s = lockstep_with
+        s.setup(init.clone(), list(w.protocol), data, list(w.lb), list(w.ub))
+        per = lockstep.lockstep_gpu(r, s, iters, w.protocol, w.lb, w.ub)
+        return r, lockstep.summarise(per)
+
+    def ours(dtype, solve):
+        s = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, dtype, solve_dtype=solve)
+        p = init.to(dtype).clone()
+        s.setup(p, list(w.protocol), data.to(dtype), list(w.lb), list(w.ub))
+        s.run(iters)
+        torch.cuda.synchronize()
+        return p, s.step_type_t[0].clone()
+
+    r, _ = reference()
+    p_ref, st_ref = r.pars.clone(), r.step_type[0].clone()
+    del r
+    p64, st64 = ours(torch.float64, torch.float64)
+    mask = (st64 == 0) & torch.all((p64 > lb_t.double()[:, None] * (1 + 1e-6) + 1e-30) &
+                                   (p64 < ub_t.double()[:, None] * (1 - 1e-6)), dim=0)
+    out = {"workload": "ivim10_8.4M (C2), 100 iterations", "voxels": n,
+           "reference": "the reference's generated LM kernel for sm_103a (oracle/_ref)",
+           "fp64_fit": "all-FP64 fitter, same LM and start, 100 iterations, tol 1e-8",
+           "fp64_converged_interior_voxels": int(mask.sum())}
+
+    def block(p, st):
+        med, frac = _median_rel_gpu(p, p_ref)
+        medm, fracm = _median_rel_gpu(p[:, mask], p_ref[:, mask])
+        m64, f64 = _median_rel_gpu(p[:, mask], p64[:, mask])
+        conv_o, conv_r = st == 0, st_ref == 0
+        both = int((conv_o & conv_r).sum())
+        return {"vs_reference": {"median_rel_err": med, "frac_voxels_gt_1e-4": frac,
+                                 "fp64_converged_interior": {"median_rel_err": medm, "frac_voxels_gt_1e-4": fracm}},
+                "vs_fp64_on_fp64_converged_interior": {"median_rel_err": m64, "frac_voxels_gt_1e-4": f64},
+                "flags_agree": float((conv_o == conv_r).double().mean()),
+                "converged": int(conv_o.sum()), "converged_reference": int(conv_r.sum()),
+                "converged_recall": both / max(1, int(conv_r.sum())),
+                "converged_precision": both / max(1, int(conv_o.sum()))}
+
+    m64r, f64r = _median_rel_gpu(p_ref[:, mask], p64[:, mask])
+    out["reference_vs_fp64_on_fp64_converged_interior"] = {"median_rel_err": m64r, "frac_voxels_gt_1e-4": f64r}
+    for name, solve in (("f32_state_f64_solve", torch.float64), ("f32_state_f32_solve", torch.float32)):
+        p, st = ours(torch.float32, solve)
+        out[name] = block(p, st)
+        del p
+        s = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float32, solve_dtype=solve)
+        r, ls = reference(lockstep_with=s)
+        out[name]["lockstep"] = ls
+        del r, s
+        torch.cuda.empty_cache()
+    return out
+
+
 # ---- GPU helpers -------------------------------------------------------------
 
 def _median_rel_gpu(a, b):
@@ -336,6 +417,71 @@ def _stage_ms(events, a, b):
     """Elapsed ms between the events named a and b of one fit's event list."""
     d = dict(events)
     return d[a].elapsed_time(d[b])
+
+
+def fallback_rule_report(run_warm, run_pre, run_plain, plain, k_warm, k_plain, ref, w, N):
+    """The implemented fallback rule against the one that needs the plain fit.
+
+    The pipeline refits a voxel when its warm fit lands on a bound, has a
+    non-finite cost, or does not end below the cost at the plain fitter's
+    constant start. The rule that compares with the plain fit's own final
+    cost needs the plain fit of every voxel, which is what the warm start
+    avoids. Here (outside every timed region) the plain LM runs at its 1e-4
+    budget on all voxels; the report counts the voxels the implemented rule
+    leaves unflagged whose warm cost ends above the plain fit's (strictly, and
+    by more than relative margins at and above the cost's fp32 resolution),
+    and the accuracy against the FP64 fit of the pipeline as run and of the
+    pipeline with the plain-cost rule applied on top (each such voxel taking
+    the plain fit). The flagged voxels are split by the criterion that flags
+    them, with the share whose refit is kept."""
+    import torch
+
+    pre_pars, pre_cost, const_cost = run_pre(k_warm)
+    lo = torch.tensor(w.lb, device=pre_pars.device)[:, None]
+    hi = torch.tensor(w.ub, device=pre_pars.device)[:, None]
+    on_bound = ((pre_pars <= lo) | (pre_pars >= hi)).any(0)
+    cost_bad = ~torch.isfinite(pre_cost) | ~(pre_cost < const_cost)
+    res = run_warm(k_warm)
+    w_pars, w_cost = res.pars.clone(), res.cost.clone()
+    n_fb = res.n_fallback
+    flagged = torch.zeros(N, dtype=torch.bool, device=w_pars.device)
+    if n_fb:
+        flagged[res.fallback_idx[:n_fb].long()] = True
+    kept = flagged & (w_pars != pre_pars).any(0)
+    p_pl = run_plain(k_plain).clone()
+    c_pl = plain.cost()
+    unflagged = ~flagged
+    cls = {}
+    for name, m in (("bound_only", on_bound & ~cost_bad), ("cost_only", cost_bad & ~on_bound),
+                    ("bound_and_cost", on_bound & cost_bad)):
+        cls[name] = {"voxels": int(m.sum()), "refit_kept": int((m & kept).sum())}
+    out = {"voxels": N, "flagged": int(flagged.sum()), "flagged_by": cls,
+           "flag_classes_consistent": bool(torch.equal(flagged, on_bound | cost_bad)),
+           "rule": "refit when the warm fit's cost is not finite or not below the cost at the constant start, "
+                   "or a parameter is on a bound"}
+    worse = {}
+    for name, margin in (("strict", 0.0), ("rel_1e-6", 1e-6), ("rel_1e-5", 1e-5), ("rel_1e-4", 1e-4),
+                         ("rel_1e-3", 1e-3)):
+        m = unflagged & (w_cost > c_pl * (1.0 + margin))
+        worse[name] = int(m.sum())
+    out["unflagged_warm_cost_above_plain"] = worse
+    out["unflagged_frac_above_plain_rel_1e-4"] = worse["rel_1e-4"] / N
+    med, frac = _median_rel_gpu(w_pars, ref)
+    above = unflagged & (w_cost > c_pl)
+    ideal = torch.where(above[None], p_pl, w_pars)
+    med_i, frac_i = _median_rel_gpu(ideal, ref)
+    out["accuracy_as_run"] = {"median_rel_err": med, "frac_voxels_gt_1e-4": frac}
+    out["accuracy_with_plain_cost_rule"] = {"median_rel_err": med_i, "frac_voxels_gt_1e-4": frac_i}
+    for name, margin in (("rel_1e-4", 1e-4), ("rel_1e-2", 1e-2)):
+        big = unflagged & (w_cost > c_pl * (1.0 + margin))
+        if int(big.sum()):
+            ew = _median_rel_gpu(w_pars[:, big], ref[:, big])
+            ep = _median_rel_gpu(p_pl[:, big], ref[:, big])
+            out[f"voxels_above_plain_{name}"] = {"voxels": int(big.sum()), "warm_median_rel_err": ew[0],
+                                                 "warm_frac_gt_1e-4": ew[1], "plain_median_rel_err": ep[0],
+                                                 "plain_frac_gt_1e-4": ep[1]}
+    del p_pl, ideal, pre_pars
+    return out
 
 
 # ---- headline: warm start vs plain LM at 1e-4 -----------------------------------
@@ -430,6 +576,21 @@ def warm_headline(args, ws, rank, local, dev):
     med_p, frac_p = _median_rel_gpu(p_plain, ref)
     pp_p = _per_param_median(p_plain, ref)
 
+    # ---- the fallback rule against the plain fit's cost (untimed) -------------
+    def run_pre(k):
+        """The warm fit before the fallback: parameters, cost, and the cost at
+        the constant start (the quantities the fallback check reads)."""
+        p = net.infer(data).clone()
+        s = SecondOrderLevenbergMarquardt(expr, None, w.M, torch.float32)
+        s.setup(p, list(w.protocol), data, list(w.lb), list(w.ub))
+        s.lam_t.fill_(lam0)
+        s.run(k)
+        c = s.cost()
+        c0 = s.cost(pipeline.init_constant(data, w.init_values))
+        return p, c, c0
+
+    fb_rule = fallback_rule_report(run_warm, run_pre, run_plain, plain, k_warm, k_plain, ref, w, N)
+
     # ---- the reference's own data-driven start (the IVIM notebook's segmented
     # log-linear fits: b <= 100 and b >= 193 s/mm^2), same fixed bounds ---------
     def run_seg(k):
@@ -493,7 +654,7 @@ def warm_headline(args, ws, rank, local, dev):
             "plain_curve": {k: v[0] for k, v in curve_plain.items()},
             "warm_accuracy": {"median_rel_err": med_w, "frac_voxels_gt_1e-4": frac_w, "per_param_median": pp_w},
             "plain_accuracy": {"median_rel_err": med_p, "frac_voxels_gt_1e-4": frac_p, "per_param_median": pp_p},
-            "fallback_voxels": n_fb, "refits_kept": n_kept, "segmented_init_lm": seg,
+            "fallback_voxels": n_fb, "refits_kept": n_kept, "fallback_rule": fb_rule, "segmented_init_lm": seg,
             "stage_ms": {k: round(v, 3) for k, v in stages.items()},
             "accuracy_reference": "all-FP64 GPU fit, same LM, constant start, 300 iterations, tol 1e-30",
         },
@@ -889,6 +1050,7 @@ def main():
     if single and not args.no_cpu:
         cpu = cpu_reference_at_tol(target_s=args.cpu_seconds)
         cpu["gpu_parity_ivim10"] = cpu_parity_ivim10()
+        cpu["parity_c2"] = parity_c2()
 
     if rank == 0:
         hbm, bf16_peak, peak_kind = _peaks()

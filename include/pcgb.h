@@ -151,6 +151,20 @@ int pcgb_lm_run_refill(pcgb_fitter* fitter, const void* consts, int64_t consts_s
                        uint32_t* work_counter, int grid, void* stream);
 
 /*
+ * pcgb_lm_run from a fresh start with only the parameters kept: the first LM
+ * stage of the warm-start pipeline (no reference counterpart). Every voxel
+ * starts at lam = lam0 (> 0) and step_type = 1 with the given params; no
+ * damping, cost or step state is read, and only params (and step_type, when
+ * not NULL) are written, so the caller allocates and initialises no other
+ * state. The arithmetic of each iteration is pcgb_lm_run's.
+ */
+int pcgb_lm_run_fresh(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                      const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                      double eta, double acc, double dec, void* params, int8_t* step_type, int64_t nprobs, int iters,
+                      const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                      double lam0, int block, void* stream);
+
+/*
  * Fallback check of a warm-started fit, fused per model (no reference
  * counterpart; it implements the rule "refit from the plain fitter's start
  * where the warm fit fails to lower the cost below that start's or lands on a
@@ -490,6 +504,18 @@ int pcgb_mlp_forward(const float* signals, int64_t n, int nin, int log_in, const
 int pcgb_mlp_forward_tc(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
                         const float* const* w_master, int nout, const int* kinds, const float* mean, const float* stdv,
                         const float* lb, const float* ub, float* out, int* status, void* stream);
+
+/* pcgb_mlp_forward_tc with its failure path exposed (no reference
+ * counterpart). wait_limit: mbarrier try_wait rounds before a wait for the
+ * tensor cores counts as lost (0 = the default, 2^22). skip_tile: a test hook
+ * for that path - the 128-voxel tile with this index (-1 = none) never has its
+ * first layer issued, so its warpgroup's wait runs out with none of its
+ * tensor-core work in flight; the kernel then sets *status to 1, stops that
+ * warpgroup's work, still frees its tensor memory and returns normally. */
+int pcgb_mlp_forward_tc_ex(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
+                           const float* const* w_master, int nout, const int* kinds, const float* mean,
+                           const float* stdv, const float* lb, const float* ub, float* out, int* status,
+                           unsigned wait_limit, int64_t skip_tile, void* stream);
 
 /* Last error of pcgb_mlp_forward_tc on this host thread. */
 const char* pcgb_mlp_tc_last_error(void);

@@ -38,6 +38,9 @@ SIGNATURES = {
                                    c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_int, c_void_p, c_int, c_void_p,
                                    c_void_p, c_int, c_void_p, c_i64, c_void_p, c_void_p]),
+    "pcgb_lm_run_fresh": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_double, c_double,
+                                  c_double, c_double, c_double, c_void_p, c_void_p, c_i64, c_int, c_void_p, c_int,
+                                  c_void_p, c_void_p, c_double, c_int, c_void_p]),
     "pcgb_lm_run_refill": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_double,
                                    c_double, c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
                                    c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_int, c_void_p, c_int, c_void_p,
@@ -106,6 +109,9 @@ SIGNATURES = {
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "pcgb_mlp_forward_tc": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
                                     c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "pcgb_mlp_forward_tc_ex": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
+                                       c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, ctypes.c_uint, c_i64,
+                                       c_void_p]),
     "pcgb_mlp_tc_last_error": (c_char_p, []),
 }
 
@@ -141,7 +147,7 @@ def lib(build_if_missing: bool = True):
 def check(fn_name: str, rc: int):
     if rc != 0:
         L = lib()
-        if fn_name.startswith("pcgb_mlp_forward_tc"):
+        if fn_name.startswith("pcgb_mlp_forward_tc"):  # also pcgb_mlp_forward_tc_ex
             err = L.pcgb_mlp_tc_last_error
         elif fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")):
             err = L.pcgb_mlp_last_error

@@ -626,7 +626,8 @@ template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHAR
 PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = Epi{}) {
   constexpr int P = Model::P, H = Model::H, C = Model::C;
   const long long N = a.N;
-  if (a.step_type[v] == 0) {
+  const bool fresh = (a.flags & PCGB_LM_FRESH) != 0;
+  if (!fresh && a.step_type[v] == 0) {
     // converged before this call (lsqnonlin.py:1000-1002): nothing changes,
     // first_f / last_f are copies of f as in the reference's host loop
     if (a.iters > 0) {
@@ -650,7 +651,7 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
     p[k] = load<TA>(a.pars, k * N + v);
     lo[k] = SHARED_B ? Num<TA>::slb(a, k) : load<TA>(a.lb, k * a.bstride + v);
     hi[k] = SHARED_B ? Num<TA>::sub(a, k) : load<TA>(a.ub, k * a.bstride + v);
-    stp[k] = a.step ? load<TA>(a.step, k * N + v) : TA(0);
+    stp[k] = !fresh && a.step ? load<TA>(a.step, k * N + v) : TA(0);
   }
   TA d[M];
 #pragma unroll
@@ -660,9 +661,9 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
 #pragma unroll
     for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
   }
-  TA lam = load<TA>(a.lam, v);
-  int st = a.step_type[v];
-  TA f = load<TA>(a.f, v);
+  TA lam = fresh ? TA(a.lam0) : load<TA>(a.lam, v);
+  int st = fresh ? 1 : a.step_type[v];
+  TA f = fresh ? TA(0) : load<TA>(a.f, v);
   TA first = f;
   const TA tol = Num<TA>::lmc(a, 0), mu = Num<TA>::lmc(a, 1), eta = Num<TA>::lmc(a, 2), acc = Num<TA>::lmc(a, 3),
              dec = Num<TA>::lmc(a, 4);
@@ -679,6 +680,11 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
   TA* pars = static_cast<TA*>(a.pars);
 #pragma unroll
   for (int k = 0; k < P; ++k) pars[k * N + v] = p[k];
+  if (a.flags & PCGB_LM_PARS_ONLY) {
+    if (a.step_type) a.step_type[v] = static_cast<signed char>(st);
+    if constexpr (Epi::kActive) epi(p, d);
+    return;
+  }
   if (a.step) {
 #pragma unroll
     for (int k = 0; k < P; ++k) static_cast<TA*>(a.step)[k * N + v] = stp[k];

@@ -7,6 +7,10 @@
 #define PCGB_MAX_PROTOCOL 256
 #define PCGB_MAX_MODELS 8
 
+// PcgbLmParams.flags of an LM run
+#define PCGB_LM_FRESH 1      // every voxel starts at lam = lam0, step_type = 1; lam, f, step are not read
+#define PCGB_LM_PARS_ONLY 2  // only pars (and step_type, when given) are written back
+
 struct PcgbLmParams {
   // structure-of-arrays, voxel index fastest; element type is the fitter's
   // state type (float, or double for the all-FP64 build)
@@ -34,7 +38,7 @@ struct PcgbLmParams {
   long long cstride;       // N: per-voxel constants; 0: protocol_* hold them
   long long bstride;       // N: per-voxel bounds; 0: shared_* hold them
   int iters;
-  int flags;
+  int flags;               // PCGB_LM_* bits
   double tol, mu, eta, acc, dec;
   float tol_f, mu_f, eta_f, acc_f, dec_f;  // the same constants rounded to float (set with them)
   // fallback check of a warm-started fit (warm_check_grid / warm_select_grid)
@@ -45,7 +49,7 @@ struct PcgbLmParams {
   int* fb_idx;                      // (N) flagged voxel indices, compacted
   unsigned int* fb_count;           // [0] flagged voxels, [1] refits kept (zeroed by the host)
   signed char* which;               // (N) 1 where the refit was kept, or null
-  double lam0;                      // damping of the refit
+  double lam0;                      // damping of the refit (PCGB_LM_FRESH: of every voxel)
   float init_val[PCGB_MAX_PARAMS];  // constant start of the refit; NaN = the voxel's largest sample
   // shared protocol and bounds in both precisions, so the kernel reads its own
   // type straight from the parameter bank (constant k of sample i at k*M + i)

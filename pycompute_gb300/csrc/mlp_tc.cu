@@ -49,7 +49,7 @@ constexpr int THREADS = NWG * 128;
 constexpr int TMEM_COLS = 512;  // >= NWG x 128 accumulator columns, a power of 2
 constexpr int LDH_G = HID + 8;  // leading dimension of the hidden weights in global memory
 constexpr int LD1_G = NIN + 8;  // ... of the first layer's weights
-constexpr unsigned kWaitLimit = 1u << 22;  // try_wait rounds before a wait counts as lost
+constexpr unsigned kWaitLimit = 1u << 22;  // default try_wait rounds before a wait counts as lost
 
 // The biases enter the accumulators through one more MMA per layer: A = a
 // 128 x 16 tile whose first two columns are 1, B = the layer's bias split
@@ -82,6 +82,8 @@ struct TcArgs {
   float mean[NOUT_MAX], stdv[NOUT_MAX], lb[NOUT_MAX], ub[NOUT_MAX];
   float* out;            // SoA (nout, n)
   int* status;           // 0 = ok, else the kernel lost an mbarrier wait (may be null)
+  unsigned wait_limit;   // try_wait rounds before a wait counts as lost
+  long long skip_tile;   // failure-path test: this tile's first layer is never issued (-1 = none)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -131,8 +133,8 @@ __device__ __forceinline__ bool wg_sync_any(int g, bool lost) {
 }
 
 // bounded wait for the phase `parity` of an mbarrier; false if it never completed
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-  for (unsigned i = 0; i < kWaitLimit; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, unsigned limit) {
+  for (unsigned i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
         "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
@@ -317,7 +319,11 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
       fence_async_smem();   // this thread's A row -> visible to the tensor cores
       fence_before_sync();  // its earlier TMEM reads are done
       wg_sync(g);
-      if (issuer) {
+      // failure-path test: the issuer skips the layer's MMAs and their commit,
+      // so the mbarrier phase never completes while no tensor-core work of this
+      // warpgroup is in flight, and the wait below runs out
+      const bool skip = layer == 0 && tile == p.skip_tile;
+      if (issuer && !skip) {
         fence_after_sync();
         if (layer == 0) {
           mma_bf16(d_tmem, smem_desc(xs, 128, 256), smem_desc(w1s, 128, 256), ID_HID, 0u);
@@ -336,7 +342,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
       }
       // one warp polls the mbarrier; the other three wait in the hardware
       // barrier below and take no issue slots from the other tiles' epilogues
-      const bool ok = (warp & 3) != 0 || mbar_wait(mbar, phase);
+      const bool ok = (warp & 3) != 0 || mbar_wait(mbar, phase, p.wait_limit);
       phase ^= 1u;
       if (wg_sync_any(g, !ok)) {
         lost = true;
@@ -379,7 +385,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
   if (lost && issuer) {
     // the lost phase may still complete: give the warpgroup's MMAs a second
     // bounded wait before the TMEM they write is returned
-    (void)mbar_wait(mbar, phase ^ 1u);
+    (void)mbar_wait(mbar, phase ^ 1u, p.wait_limit);
     if (p.status) atomicExch(p.status, 1);
   }
   // all TMEM reads done before the allocation is returned
@@ -404,6 +410,14 @@ const char* pcgb_mlp_tc_last_error(void) { return g_err.c_str(); }
 int pcgb_mlp_forward_tc(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
                         const float* const* w_master, int nout, const int* kinds, const float* mean, const float* stdv,
                         const float* lb, const float* ub, float* out, int* status, void* stream) {
+  return pcgb_mlp_forward_tc_ex(signals, n, nin, log_in, w_bf16, w_master, nout, kinds, mean, stdv, lb, ub, out,
+                                status, 0u, -1, stream);
+}
+
+int pcgb_mlp_forward_tc_ex(const float* signals, int64_t n, int nin, int log_in, const void* const* w_bf16,
+                           const float* const* w_master, int nout, const int* kinds, const float* mean,
+                           const float* stdv, const float* lb, const float* ub, float* out, int* status,
+                           unsigned wait_limit, int64_t skip_tile, void* stream) {
   g_err.clear();
   if (n < 0) {
     g_err = "n must be >= 0";
@@ -444,6 +458,8 @@ int pcgb_mlp_forward_tc(const float* signals, int64_t n, int nin, int log_in, co
   }
   a.out = out;
   a.status = status;
+  a.wait_limit = wait_limit ? wait_limit : kWaitLimit;
+  a.skip_tile = skip_tile;
   const int smem = int(sizeof(TcSmem));
   cudaError_t e = cudaFuncSetAttribute(mlp_infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) {

@@ -770,11 +770,14 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
                        const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
                        int block, const int32_t* vox_idx, int64_t n_items, void* stream,
                        uint32_t* work_counter = nullptr, int grid = 0, const uint32_t* n_items_dev = nullptr,
-                       const FallbackArgs* fb = nullptr) {
+                       const FallbackArgs* fb = nullptr, int flags = 0, double lam0 = 0.0) {
   g_err.clear();
   if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
   if (nprobs < 0 || iters < 0) return fail(PCGB_EINVAL, "nprobs and iters must be >= 0");
-  if (nprobs > 0 && (!data || !params || !lam || !step_type || !f || !first_f || !last_f))
+  const bool fresh = flags == (PCGB_LM_FRESH | PCGB_LM_PARS_ONLY);
+  if (nprobs > 0 && fresh && (!data || !params))
+    return fail(PCGB_EINVAL, "data and params are required");
+  if (nprobs > 0 && !fresh && (!data || !params || !lam || !step_type || !f || !first_f || !last_f))
     return fail(PCGB_EINVAL, "data, params, lam, step_type, f, first_f and last_f are required");
   if (int rc = check_device(ft)) return rc;
   PcgbLmParams prm;
@@ -807,6 +810,8 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
   prm.N = nprobs;
   prm.bstride = bounds_stride;
   prm.iters = iters;
+  prm.flags = flags;
+  if (fresh) prm.lam0 = lam0;
   set_lm_constants(prm, tol, mu, eta, acc, dec);
   const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_LM_C1_B1 : K_LM_C1_B0)
                                              : (bounds_stride == 0 ? K_LM_C0_B1 : K_LM_C0_B0);
@@ -891,6 +896,19 @@ int pcgb_lm_run(pcgb_fitter* ft, const void* consts, int64_t consts_stride, cons
   return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
                      params, step, lam, step_type, f, first_f, last_f, iters_done, nprobs, iters, protocol_host,
                      protocol_len, lb_host, ub_host, block, nullptr, 0, stream);
+}
+
+int pcgb_lm_run_fresh(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                      const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                      double eta, double acc, double dec, void* params, int8_t* step_type, int64_t nprobs, int iters,
+                      const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                      double lam0, int block, void* stream) {
+  g_err.clear();
+  if (!(lam0 > 0.0)) return fail(PCGB_EINVAL, "lam0 must be > 0");
+  return lm_run_impl(ft, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride, tol, mu, eta, acc, dec,
+                     params, nullptr, nullptr, step_type, nullptr, nullptr, nullptr, nullptr, nprobs, iters,
+                     protocol_host, protocol_len, lb_host, ub_host, block, nullptr, 0, stream, nullptr, 0, nullptr,
+                     nullptr, PCGB_LM_FRESH | PCGB_LM_PARS_ONLY, lam0);
 }
 
 int pcgb_lm_run_refill(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,

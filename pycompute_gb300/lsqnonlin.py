@@ -258,8 +258,13 @@ class SecondOrderLevenbergMarquardt:
     def get_kernel_funcid(self):
         return "k_" + self.funcid
 
-    def setup(self, pars_t, consts_t, data_t, lower_bound_t, upper_bound_t):
-        """Bind caller-owned arrays and allocate the fitter state (lsqnonlin.py:1036-1056)."""
+    def setup(self, pars_t, consts_t, data_t, lower_bound_t, upper_bound_t, init_state: bool = True):
+        """Bind caller-owned arrays and allocate the fitter state (lsqnonlin.py:1036-1056).
+
+        ``init_state=False`` (no reference counterpart) allocates the damping,
+        step-code and cost arrays without initialising them and keeps no step
+        or iteration-count arrays: for callers whose next call is run_fresh(),
+        which reads none of that state (the warm-start pipeline)."""
         pars_t = _as_tensor(pars_t, "pars_t")
         data_t = _as_tensor(data_t, "data_t")
         P, M, C = self.nparam, self.ndata, self.nconst
@@ -301,11 +306,18 @@ class SecondOrderLevenbergMarquardt:
         dev = pars_t.device
         self.first_f = torch.empty((1, N), dtype=self.dtype, device=dev)
         self.last_f = torch.empty((1, N), dtype=self.dtype, device=dev)
-        self.lam_t = torch.full((1, N), 5.0, dtype=self.dtype, device=dev)
-        self.step_t = torch.zeros((P, N), dtype=self.dtype, device=dev)
-        self.f_t = torch.zeros((1, N), dtype=self.dtype, device=dev)
-        self.step_type_t = torch.ones((1, N), dtype=torch.int8, device=dev)
-        self.iters_t = torch.zeros((1, N), dtype=torch.int32, device=dev)
+        if init_state:
+            self.lam_t = torch.full((1, N), 5.0, dtype=self.dtype, device=dev)
+            self.step_t = torch.zeros((P, N), dtype=self.dtype, device=dev)
+            self.f_t = torch.zeros((1, N), dtype=self.dtype, device=dev)
+            self.step_type_t = torch.ones((1, N), dtype=torch.int8, device=dev)
+            self.iters_t = torch.zeros((1, N), dtype=torch.int32, device=dev)
+        else:
+            self.lam_t = torch.empty((1, N), dtype=self.dtype, device=dev)
+            self.f_t = torch.empty((1, N), dtype=self.dtype, device=dev)
+            self.step_type_t = torch.empty((1, N), dtype=torch.int8, device=dev)
+            self.step_t = None
+            self.iters_t = None
         with torch.cuda.device(dev):
             self.build()
 
@@ -351,6 +363,23 @@ class SecondOrderLevenbergMarquardt:
                 _ptr(self.pars_t), _ptr(self.step_t), _ptr(self.lam_t), _ptr(self.step_type_t), _ptr(self.f_t),
                 _ptr(self.first_f), _ptr(self.last_f), _ptr(self.iters_t), self.Nprobs, int(iters), pv, plen,
                 lbh if self._bstride == 0 else None, ubh if self._bstride == 0 else None, int(block))
+
+    def run_fresh(self, iters: int, lam0: float, tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0, block: int = 0):
+        """``iters`` iterations from a fresh start at damping ``lam0`` and
+        step code 1 on every voxel, keeping only the parameters and step codes
+        (pcgb_lm_run_fresh; no reference counterpart): the damping, cost and
+        step arrays are neither read nor written."""
+        with torch.cuda.device(self.pars_t.device):
+            pv, plen = self._proto_args()
+            lbh = (ctypes.c_double * self.nparam)(*(self._lb_host or [0.0] * self.nparam))
+            ubh = (ctypes.c_double * self.nparam)(*(self._ub_host or [0.0] * self.nparam))
+            rc = _lib.lib().pcgb_lm_run_fresh(
+                self.build().handle, _ptr(self.consts_t), self._cstride, _ptr(self.data_t), _ptr(self.lower_bound_t),
+                _ptr(self.upper_bound_t), self._bstride, float(tol), float(mu), float(eta), float(acc), float(dec),
+                _ptr(self.pars_t), _ptr(self.step_type_t), self.Nprobs, int(iters), pv, plen,
+                lbh if self._bstride == 0 else None, ubh if self._bstride == 0 else None, float(lam0), int(block),
+                ctypes.c_void_p(_stream_ptr()))
+            _lib.check("pcgb_lm_run_fresh", rc)
 
     def run_check(self, iters: int, init_values, lam_refit: float, cost, pars_backup, cost_backup, fb_idx, fb_count,
                   tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0, block: int = 0):

@@ -290,8 +290,13 @@ class WarmStartFitter:
         pars = self.net.infer(data, out=pars_out)
         mark("network")
         solm = self._fitter()
-        solm.setup(pars, prot, data, lb, ub)
-        solm.lam_t.fill_(lam0)
+        if fused == "select":
+            # the warm LM reads no state and keeps only the parameters and step
+            # codes; the check initialises the state of the voxels it flags
+            solm.setup(pars, prot, data, lb, ub, init_state=False)
+        else:
+            solm.setup(pars, prot, data, lb, ub)
+            solm.lam_t.fill_(lam0)
         mark("setup")
         if fused in ("epilogue", "select"):
             b = self._buffers(P, N, dev)
@@ -301,7 +306,7 @@ class WarmStartFitter:
                 mark("lm_warm")
                 mark("check")
             else:
-                solm.run(iters_warm)
+                solm.run_fresh(iters_warm, lam0)
                 mark("lm_warm")
                 self._warm_check(solm, data, pars, b)
                 mark("check")
@@ -313,7 +318,7 @@ class WarmStartFitter:
                 torch.cuda.synchronize()
                 for (n0, e0), (n1, e1) in zip(ev[:-1], ev[1:]):
                     timings[n1] = timings.get(n1, 0.0) + e0.elapsed_time(e1)
-            return WarmFit(pars, b["cost"], b["counts"], solm.step_type_t)
+            return WarmFit(pars, b["cost"], b["counts"], solm.step_type_t, b["idx"])
         solm.run(iters_warm)
         mark("lm_warm")
         if fused:
@@ -334,7 +339,7 @@ class WarmStartFitter:
                 torch.cuda.synchronize()
                 for (n0, e0), (n1, e1) in zip(ev[:-1], ev[1:]):
                     timings[n1] = timings.get(n1, 0.0) + e0.elapsed_time(e1)
-            return WarmFit(pars, b["cost"], b["counts"], solm.step_type_t)
+            return WarmFit(pars, b["cost"], b["counts"], solm.step_type_t, b["idx"])
         cost = solm.cost()
         # cost at the plain fitter's starting point
         p0 = init_constant(data, w.init_values)
@@ -390,10 +395,13 @@ def copy_rows(dst: torch.Tensor, dst_col: int, src: torch.Tensor, src_col: int, 
 
 class WarmFit:
     """Result of WarmStartFitter.fit: pars (P, N), cost (N), step_type (1, N)
-    on the device; n_fallback / n_refit_kept read the device counters (a sync)."""
+    on the device; fallback_idx (int32, N) lists the flagged voxels in its
+    first n_fallback entries (None for the unfused pipeline); n_fallback /
+    n_refit_kept read the device counters (a sync)."""
 
-    def __init__(self, pars, cost, counts, step_type):
+    def __init__(self, pars, cost, counts, step_type, fallback_idx=None):
         self.pars, self.cost, self.counts, self.step_type = pars, cost, counts, step_type
+        self.fallback_idx = fallback_idx
 
     @property
     def n_fallback(self) -> int:

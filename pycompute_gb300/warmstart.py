@@ -291,3 +291,9 @@ class WarmStartMLP:
         """Nonzero if a tcgen05 inference gave up on a bounded wait (reads the device flag)."""
         st = getattr(self, "_status", None)
         return 0 if st is None else int(st.item())
+
+    def clear_tc_status(self):
+        """Reset the device flag that tc_status() reads (it stays set once set)."""
+        st = getattr(self, "_status", None)
+        if st is not None:
+            st.zero_()

@@ -171,3 +171,45 @@ def test_gelu_recipe_matches_oracle():
     assert np.isclose(dg, want_d, rtol=1e-5, atol=1e-6).mean() > 0.95
     assert np.all(np.abs(dg - want_d) <= tol), np.max(np.abs(dg - want_d) / tol)
     assert g[np.where(z == 40.0)[0][0]] == 40.0 and g[np.where(z == -40.0)[0][0]] == 0.0
+
+
+def test_tcgen05_lost_wait_sets_status_frees_tmem_and_returns():
+    """The failure path of the tcgen05 network kernel, made to run without any
+    fault: through pcgb_mlp_forward_tc_ex, the issuing thread of the warpgroup
+    that owns tile 0 never issues that tile's first layer nor its commit, so
+    the layer's mbarrier phase never completes while none of that warpgroup's
+    tensor-core work is in flight. With a short wait limit the wait runs out:
+    the call returns normally, the status word reads 1 and the other tiles
+    are still computed. A normal inference right after it must succeed and
+    equal the mma.sync kernel on every voxel, which it could not if the tensor
+    memory of the failed launch had not been freed (every CTA allocates all
+    512 columns of its SM)."""
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    n = 128 * 12 + 77  # 13 tiles on 4 CTAs (one tile per warpgroup), a ragged last tile
+    true, data, *_ = w.generate(n, seed=13)
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], w.lb, w.ub, DEV, seed=8, log_in=True)
+    sig = torch.from_numpy(np.ascontiguousarray(data)).to(DEV)
+    net.fit_normalisation(sig, torch.from_numpy(np.ascontiguousarray(true)).to(DEV))
+    want = net.infer(sig, impl="mma")
+    out = torch.full((4, n), -1.0, device=DEV)
+    status = torch.zeros(1, dtype=torch.int32, device=DEV)
+    wb = (ctypes.c_void_p * 4)(*[L.wbf.data_ptr() for L in net.layers])
+    wm = (ctypes.c_void_p * 4)(*[L.master.data_ptr() for L in net.layers])
+    kinds = (ctypes.c_int * 4)(*net.kinds)
+    fl = lambda v: (ctypes.c_float * 4)(*[float(x) for x in v])  # noqa: E731
+    p = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    rc = _lib.lib().pcgb_mlp_forward_tc_ex(p(sig), n, 16, 1, wb, wm, 4, kinds, fl(net.mean), fl(net.std), fl(net.lb),
+                                           fl(net.ub), p(out), p(status), 1 << 12, 0,
+                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    _lib.check("pcgb_mlp_forward_tc_ex", rc)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 1
+    # tile 0 was never computed; every other tile (other warpgroups and CTAs) was
+    got, ref = out.cpu().numpy(), want.cpu().numpy()
+    assert np.all(got[:, :128] == -1.0)
+    np.testing.assert_allclose(got[:, 128:], ref[:, 128:], rtol=1e-2, atol=1e-7)
+    net.clear_tc_status()
+    again = net.infer(sig, impl="tcgen05")
+    torch.cuda.synchronize()
+    assert net.tc_status() == 0
+    np.testing.assert_allclose(again.cpu().numpy(), ref, rtol=1e-2, atol=1e-7)
