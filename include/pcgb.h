@@ -187,6 +187,25 @@ int pcgb_warm_check(pcgb_fitter* fitter, const void* consts, int64_t consts_stri
                     int64_t nprobs, void* stream);
 
 /*
+ * The first LM stage of a warm-started fit and its fallback check in one
+ * launch (no reference counterpart): pcgb_lm_run_fresh for `iters`
+ * iterations from params at damping lam_start (> 0), then, per voxel and
+ * from registers, the rule and outputs of pcgb_warm_check. The warm fit's
+ * cost is the one the iterations evaluated at the final parameters (NaN in
+ * cost and cost_backup where they did not: the last accepted step was moved
+ * by a bound, which flags the voxel; the select evaluates such a cost), so
+ * only the cost at the constant start is computed. block: threads per block
+ * (0 = default). nprobs < 2^31.
+ */
+int pcgb_warm_lm_check(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, int iters, double lam_start, const double* protocol_host,
+                       int protocol_len, const double* lb_host, const double* ub_host, const double* init_values,
+                       double lam0, void* params, void* lam, int8_t* step_type, void* f, void* cost,
+                       void* pars_backup, void* cost_backup, int32_t* fb_idx, uint32_t* fb_count, int64_t nprobs,
+                       int block, void* stream);
+
+/*
  * pcgb_lm_run with pcgb_warm_check as its epilogue, in one launch: the check
  * runs on the samples and the fit still in registers (no second pass over the
  * signals). Arguments as in pcgb_lm_run followed by those of pcgb_warm_check;

@@ -58,6 +58,10 @@ SIGNATURES = {
     "pcgb_warm_check": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_int,
                                 c_void_p, c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_void_p,
                                 c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
+    "pcgb_warm_lm_check": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64, c_double,
+                                   c_double, c_double, c_double, c_double, c_int, c_double, c_void_p, c_int, c_void_p,
+                                   c_void_p, c_void_p, c_double, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_int, c_void_p]),
     "pcgb_warm_select": (c_int, [c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_int, c_void_p, c_void_p, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
     "pcgb_f_run_subset": (c_int, [c_void_p, c_void_p, c_void_p, c_i64, c_void_p, c_void_p, c_void_p, c_i64,

@@ -86,6 +86,7 @@ template <> struct Num<float> {
   static PCGB_HD float slb(const PcgbLmParams& a, int k) { return a.shared_lb_f[k]; }
   static PCGB_HD float sub(const PcgbLmParams& a, int k) { return a.shared_ub_f[k]; }
   static PCGB_HD float inf() { return __int_as_float(0x7f800000); }
+  static PCGB_HD float nan() { return __int_as_float(0x7fffffff); }
   // tol, mu, eta, acc, dec (k = 0..4)
   static PCGB_HD float lmc(const PcgbLmParams& a, int k) {
     return k == 0 ? a.tol_f : k == 1 ? a.mu_f : k == 2 ? a.eta_f : k == 3 ? a.acc_f : a.dec_f;
@@ -99,6 +100,7 @@ template <> struct Num<double> {
   static PCGB_HD double slb(const PcgbLmParams& a, int k) { return a.shared_lb_d[k]; }
   static PCGB_HD double sub(const PcgbLmParams& a, int k) { return a.shared_ub_d[k]; }
   static PCGB_HD double inf() { return __longlong_as_double(0x7ff0000000000000LL); }
+  static PCGB_HD double nan() { return __longlong_as_double(0x7fffffffffffffffLL); }
   static PCGB_HD double lmc(const PcgbLmParams& a, int k) {
     return k == 0 ? a.tol : k == 1 ? a.mu : k == 2 ? a.eta : k == 3 ? a.acc : a.dec;
   }
@@ -406,12 +408,17 @@ constexpr int sample_unroll() { return SameType<TA, float>::value && SameType<TS
 
 // The iterations of one voxel on register state (lsqnonlin.py:823-924 per
 // iteration). cf(k, i) returns constant k of sample i; first receives the cost
-// of the first iteration; done counts the iterations run.
+// of the first iteration; done counts the iterations run; fend receives the
+// cost at the final parameters where an iteration evaluated it (the cost of
+// the last iterate when its step was rejected or the voxel converged, the
+// trial cost when the step was accepted and no bound moved the point), NaN
+// otherwise.
 template <class Model, int M, typename TA, typename TS, class CF>
 PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const TA (&lo)[Model::P],
                         const TA (&hi)[Model::P], TA (&stp)[Model::P], TA& lam, int& st, TA& f, TA& first, int& done,
-                        int iters, TA tol, TA mu, TA eta, TA acc, TA dec) {
+                        int iters, TA tol, TA mu, TA eta, TA acc, TA dec, TA& fend) {
   constexpr int P = Model::P, H = Model::H, C = Model::C;
+  fend = Num<TA>::nan();
   for (int it = 0; it < iters; ++it) {
     if (st == 0) break;
     ++done;
@@ -449,6 +456,7 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
       }
     }
     f = fa;
+    fend = f;
     if (it == 0) first = f;
 
     // damped solve in TS (lsqnonlin.py:848-878), then drop NaN/Inf (881-891)
@@ -576,6 +584,7 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
     if (accept) {
 #pragma unroll
       for (int k = 0; k < P; ++k) p[k] = pt[k];
+      fend = ftp;
       if (very_good) {
         lam *= acc;
         st = 1;
@@ -591,15 +600,28 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
       st |= 8;
     }
     // box projection (lsqnonlin.py:590-601)
+    bool moved = false;
 #pragma unroll
     for (int k = 0; k < P; ++k) {
-      if (p[k] > hi[k])
+      if (p[k] > hi[k]) {
         p[k] = hi[k];
-      else if (p[k] < lo[k])
+        moved = true;
+      } else if (p[k] < lo[k]) {
         p[k] = lo[k];
+        moved = true;
+      }
     }
+    if (moved) fend = Num<TA>::nan();
   }
+}
 
+// lm_iterate for callers that do not need the cost at the final parameters
+template <class Model, int M, typename TA, typename TS, class CF>
+PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const TA (&lo)[Model::P],
+                        const TA (&hi)[Model::P], TA (&stp)[Model::P], TA& lam, int& st, TA& f, TA& first, int& done,
+                        int iters, TA tol, TA mu, TA eta, TA acc, TA dec) {
+  TA fend;
+  lm_iterate<Model, M, TA, TS>(cf, d, p, lo, hi, stp, lam, st, f, first, done, iters, tol, mu, eta, acc, dec, fend);
 }
 
 // protocol accessors for lm_iterate
@@ -614,14 +636,15 @@ template <typename TA, int M, int NC> struct RegConsts {
 
 // No epilogue after a voxel's fit.
 struct NoEpilogue {
-  template <class PArr, class DArr>
-  PCGB_HD void operator()(const PArr&, const DArr&) const {}
+  template <class PArr, class DArr, class T>
+  PCGB_HD void operator()(const PArr&, const DArr&, T) const {}
   static constexpr bool kActive = false;
 };
 
-// All iterations of one voxel; then epi(p, d) with the final parameters and
-// the samples still in registers (a voxel converged before the call loads
-// them for the epilogue).
+// All iterations of one voxel; then epi(p, d, fend) with the final parameters
+// and the samples still in registers and the cost at the final parameters
+// where the iterations evaluated it (NaN otherwise; see lm_iterate). A voxel
+// converged before the call loads p and d for the epilogue.
 template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B, class Epi = NoEpilogue>
 PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = Epi{}) {
   constexpr int P = Model::P, H = Model::H, C = Model::C;
@@ -641,7 +664,7 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
       for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * N + v);
 #pragma unroll
       for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
-      epi(p, d);
+      epi(p, d, Num<TA>::nan());
     }
     return;
   }
@@ -661,20 +684,21 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
 #pragma unroll
     for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
   }
-  TA lam = fresh ? TA(a.lam0) : load<TA>(a.lam, v);
+  TA lam = fresh ? TA(a.lam_start) : load<TA>(a.lam, v);
   int st = fresh ? 1 : a.step_type[v];
   TA f = fresh ? TA(0) : load<TA>(a.f, v);
   TA first = f;
   const TA tol = Num<TA>::lmc(a, 0), mu = Num<TA>::lmc(a, 1), eta = Num<TA>::lmc(a, 2), acc = Num<TA>::lmc(a, 3),
              dec = Num<TA>::lmc(a, 4);
   int done = 0;
+  TA fend;
 
   if constexpr (SHARED_C) {
     lm_iterate<Model, M, TA, TS>(SharedConsts<TA, M>{a}, d, p, lo, hi, stp, lam, st, f, first, done, a.iters, tol, mu,
-                                 eta, acc, dec);
+                                 eta, acc, dec, fend);
   } else {
     lm_iterate<Model, M, TA, TS>(RegConsts<TA, M, (C > 0 ? C * M : 1)>{cv}, d, p, lo, hi, stp, lam, st, f, first,
-                                 done, a.iters, tol, mu, eta, acc, dec);
+                                 done, a.iters, tol, mu, eta, acc, dec, fend);
   }
 
   TA* pars = static_cast<TA*>(a.pars);
@@ -682,7 +706,7 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
   for (int k = 0; k < P; ++k) pars[k * N + v] = p[k];
   if (a.flags & PCGB_LM_PARS_ONLY) {
     if (a.step_type) a.step_type[v] = static_cast<signed char>(st);
-    if constexpr (Epi::kActive) epi(p, d);
+    if constexpr (Epi::kActive) epi(p, d, fend);
     return;
   }
   if (a.step) {
@@ -697,7 +721,7 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
     static_cast<TA*>(a.last_f)[v] = f;
   }
   if (a.iters_done) a.iters_done[v] += done;
-  if constexpr (Epi::kActive) epi(p, d);
+  if constexpr (Epi::kActive) epi(p, d, fend);
 }
 
 // ---- refill schedule -----------------------------------------------------------
@@ -1077,15 +1101,89 @@ __device__ void lm_check_grid(const PcgbLmParams& a) {
   warm_check_voxel<Model, M, TA, SHARED_C>(a, v, valid, s.p, s.d);
 }
 
+// The check of one voxel as the epilogue of its warm LM fit (lm_warm_grid):
+// the cost at the warm fit comes from the iterations (c, NaN where they did
+// not evaluate it: the last accepted step was moved by a bound, and the voxel
+// is flagged for being on the bound anyway), so only the cost at the constant
+// start is evaluated. Same rule, compaction, backup and state reset as
+// warm_check_voxel; the flagged voxels of each group of lanes that reaches
+// this point together are compacted with one atomic (any grouping gives a
+// valid list).
+template <class Model, int M, typename TA, bool SHARED_C>
+__device__ void warm_flag_voxel(const PcgbLmParams& a, long long v, const TA (&p)[Model::P], const TA (&d)[M], TA c) {
+  constexpr int P = Model::P;
+  const long long N = a.N;
+  TA p0[P];
+  TA mx = -Num<TA>::inf();
+#pragma unroll
+  for (int i = 0; i < M; ++i) mx = fmax(mx, d[i]);
+#pragma unroll
+  for (int k = 0; k < P; ++k) p0[k] = isnan(a.init_val[k]) ? mx : TA(a.init_val[k]);
+  const TA c0 = voxel_cost<Model, M, TA, SHARED_C>(a, v, p0, d);
+  bool flag = !isfinite(c) || !(c < c0);
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    const TA lo = a.bstride ? load<TA>(a.lb, k * a.bstride + v) : Num<TA>::slb(a, k);
+    const TA hi = a.bstride ? load<TA>(a.ub, k * a.bstride + v) : Num<TA>::sub(a, k);
+    flag = flag || !(p[k] > lo) || !(p[k] < hi);
+  }
+  static_cast<TA*>(a.cost)[v] = c;
+  const unsigned m = __activemask();
+  const unsigned ballot = __ballot_sync(m, flag);
+  if (!ballot) return;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned leader = unsigned(__ffs(m) - 1);
+  unsigned base = 0;
+  if (lane == leader) base = atomicAdd(a.fb_count, (unsigned)__popc(ballot));
+  base = __shfl_sync(m, base, leader);
+  if (!flag) return;
+  const long long i = (long long)base + __popc(ballot & ((1u << lane) - 1u));
+  a.fb_idx[i] = int(v);
+#pragma unroll
+  for (int k = 0; k < P; ++k) {
+    static_cast<TA*>(a.pars_backup)[k * N + i] = p[k];
+    static_cast<TA*>(a.pars)[k * N + v] = p0[k];
+  }
+  static_cast<TA*>(a.cost_backup)[i] = c;
+  static_cast<TA*>(a.lam)[v] = TA(a.lam0);
+  a.step_type[v] = 1;
+  static_cast<TA*>(a.f)[v] = TA(0);
+}
+
+template <class Model, int M, typename TA, bool SHARED_C>
+struct FlagEpilogue {
+  const PcgbLmParams& a;
+  long long v;
+  static constexpr bool kActive = true;
+  PCGB_HD void operator()(const TA (&p)[Model::P], const TA (&d)[M], TA c) const {
+    warm_flag_voxel<Model, M, TA, SHARED_C>(a, v, p, d, c);
+  }
+};
+
+// The warm LM (a.flags: fresh start, parameters only) with the fallback check
+// as its epilogue; one thread per voxel, grid covering N.
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B>
+__device__ void lm_warm_grid(const PcgbLmParams& a) {
+  const long long v = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (v < a.N) lm_fit_voxel<Model, M, TA, TS, SHARED_C, SHARED_B>(a, v, FlagEpilogue<Model, M, TA, SHARED_C>{a, v});
+}
+
 // keep the refit or restore the warm fit of flagged item i (voxel v), from
-// the refit's parameters and samples in registers
+// the refit's parameters and samples in registers; a warm cost saved as NaN
+// (not evaluated by the warm iterations) is evaluated here
 template <class Model, int M, typename TA, bool SHARED_C>
 __device__ void warm_select_voxel(const PcgbLmParams& a, long long i, long long v, const TA (&p)[Model::P],
                                   const TA (&d)[M]) {
   constexpr int P = Model::P;
   const long long N = a.N;
   const TA c = voxel_cost<Model, M, TA, SHARED_C>(a, v, p, d);
-  const TA cb = load<TA>(a.cost_backup, i);
+  TA cb = load<TA>(a.cost_backup, i);
+  if (isnan(cb)) {
+    TA pb[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) pb[k] = load<TA>(a.pars_backup, k * N + i);
+    cb = voxel_cost<Model, M, TA, SHARED_C>(a, v, pb, d);
+  }
   const bool refit = c < cb;
   if (!refit) {
 #pragma unroll
@@ -1133,7 +1231,7 @@ struct SelectEpilogue {
   const PcgbLmParams& a;
   long long i, v;
   static constexpr bool kActive = true;
-  PCGB_HD void operator()(const TA (&p)[Model::P], const TA (&d)[M]) const {
+  PCGB_HD void operator()(const TA (&p)[Model::P], const TA (&d)[M], TA) const {
     warm_select_voxel<Model, M, TA, SHARED_C>(a, i, v, p, d);
   }
 };

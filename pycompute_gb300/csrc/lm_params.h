@@ -8,7 +8,7 @@
 #define PCGB_MAX_MODELS 8
 
 // PcgbLmParams.flags of an LM run
-#define PCGB_LM_FRESH 1      // every voxel starts at lam = lam0, step_type = 1; lam, f, step are not read
+#define PCGB_LM_FRESH 1      // every voxel starts at lam = lam_start, step_type = 1; lam, f, step are not read
 #define PCGB_LM_PARS_ONLY 2  // only pars (and step_type, when given) are written back
 
 struct PcgbLmParams {
@@ -49,7 +49,8 @@ struct PcgbLmParams {
   int* fb_idx;                      // (N) flagged voxel indices, compacted
   unsigned int* fb_count;           // [0] flagged voxels, [1] refits kept (zeroed by the host)
   signed char* which;               // (N) 1 where the refit was kept, or null
-  double lam0;                      // damping of the refit (PCGB_LM_FRESH: of every voxel)
+  double lam0;                      // damping of the refit
+  double lam_start;                 // starting damping of every voxel under PCGB_LM_FRESH
   float init_val[PCGB_MAX_PARAMS];  // constant start of the refit; NaN = the voxel's largest sample
   // shared protocol and bounds in both precisions, so the kernel reads its own
   // type straight from the parameter bank (constant k of sample i at k*M + i)

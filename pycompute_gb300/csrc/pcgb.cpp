@@ -58,7 +58,8 @@ enum KernelSlot {
   K_LM_C1_B1, K_LM_C1_B0, K_LM_C0_B1, K_LM_C0_B0, K_COST_C1, K_COST_C0, K_GMW, K_EVAL_C1, K_EVAL_C0,
   K_SEARCH_C1, K_SEARCH_C0, K_RS_C1_B1, K_RS_C1_B0, K_RS_C0_B1, K_RS_C0_B0,
   K_LMQ_C1_B1, K_LMQ_C1_B0, K_LMQ_C0_B1, K_LMQ_C0_B0, K_CHECK_C1, K_CHECK_C0, K_SELECT_C1, K_SELECT_C0,
-  K_LMC_C1_B1, K_LMC_C1_B0, K_LMC_C0_B1, K_LMC_C0_B0, K_LMS_C1_B1, K_LMS_C1_B0, K_LMS_C0_B1, K_LMS_C0_B0, K_COUNT
+  K_LMC_C1_B1, K_LMC_C1_B0, K_LMC_C0_B1, K_LMC_C0_B0, K_LMS_C1_B1, K_LMS_C1_B0, K_LMS_C0_B1, K_LMS_C0_B0,
+  K_LMW_C1_B1, K_LMW_C1_B0, K_LMW_C0_B1, K_LMW_C0_B0, K_COUNT
 };
 const char* kKernelNames[K_COUNT] = {"pcgb_lm_c1_b1", "pcgb_lm_c1_b0", "pcgb_lm_c0_b1", "pcgb_lm_c0_b0",
                                      "pcgb_cost_c1",  "pcgb_cost_c0",  "pcgb_gmw81",    "pcgb_eval_c1",
@@ -67,7 +68,8 @@ const char* kKernelNames[K_COUNT] = {"pcgb_lm_c1_b1", "pcgb_lm_c1_b0", "pcgb_lm_
                                      "pcgb_lmq_c1_b0", "pcgb_lmq_c0_b1", "pcgb_lmq_c0_b0", "pcgb_check_c1",
                                      "pcgb_check_c0", "pcgb_select_c1", "pcgb_select_c0", "pcgb_lmc_c1_b1",
                                      "pcgb_lmc_c1_b0", "pcgb_lmc_c0_b1", "pcgb_lmc_c0_b0", "pcgb_lms_c1_b1",
-                                     "pcgb_lms_c1_b0", "pcgb_lms_c0_b1", "pcgb_lms_c0_b0"};
+                                     "pcgb_lms_c1_b0", "pcgb_lms_c0_b1", "pcgb_lms_c0_b0", "pcgb_lmw_c1_b1",
+                                     "pcgb_lmw_c1_b0", "pcgb_lmw_c0_b1", "pcgb_lmw_c0_b0"};
 
 constexpr int kDefaultBlock = 128;
 constexpr int kMaxBlock = 256;
@@ -79,8 +81,8 @@ constexpr int64_t kMaxMultiChunks = int64_t(1) << 31;
 struct pcgb_fitter {
   int P = 0, C = 0, M = 0, dtype = 0, sdtype = 0;
   int device = -1;
-  cudaLibrary_t lib[4] = {};  // one per kernel group, loaded on first use
-  int lm_min_blocks[4] = {};  // occupancy hint the group's LM kernels were built with (0: none)
+  cudaLibrary_t lib[5] = {};  // one per kernel group, loaded on first use
+  int lm_min_blocks[5] = {};  // occupancy hint the group's LM kernels were built with (0: none)
   cudaKernel_t k[K_COUNT] = {};
   std::string source, structname, cache_dir;
   std::mutex mu;
@@ -93,12 +95,15 @@ namespace {
 // group is first needed: 0 the fit itself (LM, cost, model evaluation, GMW81
 // solve), 1 the searches, 2 the refill schedule and the warm-start fallback
 // check (also as the LM's epilogue), 3 the fallback refit with the select as
-// its epilogue. A group's LM kernels share one register cap (dropped when one
-// of them would spill too much), so the refit sits apart from the kernels
-// whose larger state cannot take the cap.
-constexpr int kGroups = 4;
+// its epilogue, 4 the warm LM from a fresh start with the check as its
+// epilogue. A group's LM kernels share one register cap (dropped when one of
+// them would spill too much), so the refit and the fresh warm LM sit apart
+// from the kernels whose larger state cannot take the cap.
+constexpr int kGroups = 5;
 int group_of(int slot) {
   switch (slot) {
+    case K_LMW_C1_B1: case K_LMW_C1_B0: case K_LMW_C0_B1: case K_LMW_C0_B0:
+      return 4;
     case K_SEARCH_C1: case K_SEARCH_C0: case K_RS_C1_B1: case K_RS_C1_B0: case K_RS_C0_B1: case K_RS_C0_B0:
       return 1;
     case K_LMQ_C1_B1: case K_LMQ_C1_B0: case K_LMQ_C0_B1: case K_LMQ_C0_B0: case K_CHECK_C1: case K_CHECK_C0:
@@ -117,7 +122,8 @@ int group_of(int slot) {
 // to hide the FP64 pipe's latency); a model whose capped kernels would spill
 // more than kLmMaxSpillBytes per thread is rebuilt without the cap.
 bool is_lm_slot(int slot) {
-  return slot == K_LM_C1_B1 || slot == K_LMQ_C1_B1 || slot == K_LMC_C1_B1 || slot == K_LMS_C1_B1;
+  return slot == K_LM_C1_B1 || slot == K_LMQ_C1_B1 || slot == K_LMC_C1_B1 || slot == K_LMS_C1_B1 ||
+         slot == K_LMW_C1_B1;
 }
 
 constexpr int kLmMinBlocks = 6;
@@ -143,7 +149,7 @@ std::string program_source(const char* model_source, const char* model_struct, i
   const std::string lmb = lm_min_blocks > 0 ? "__launch_bounds__(" + std::to_string(kLmMaxThreads) + ", " +
                                                   std::to_string(lm_min_blocks) + ")"
                                             : std::string(bounds);
-  const bool g0 = group == 0, g1 = group == 1, g2 = group == 2, g3 = group == 3;
+  const bool g0 = group == 0, g1 = group == 1, g2 = group == 2, g3 = group == 3, g4 = group == 4;
   for (int c = 1; c >= 0 && g0; --c)
     for (int b = 1; b >= 0; --b)
       s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lm_c" << c << "_b" << b
@@ -170,6 +176,11 @@ std::string program_source(const char* model_source, const char* model_struct, i
     for (int b = 1; b >= 0; --b)
       s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lms_c" << c << "_b" << b
         << "(const PcgbLmParams a) { pcgb::lm_select_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
+        << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
+  for (int c = 1; c >= 0 && g4; --c)
+    for (int b = 1; b >= 0; --b)
+      s << "extern \"C\" __global__ void " << (c && b ? lmb : std::string(bounds)) << " pcgb_lmw_c" << c << "_b" << b
+        << "(const PcgbLmParams a) { pcgb::lm_warm_grid<PcgbModel, " << M << ", " << ta << ", " << ts << ", "
         << (c ? "true" : "false") << ", " << (b ? "true" : "false") << ">(a); }\n";
   for (int c = 1; c >= 0 && g1; --c)
     s << "extern \"C\" __global__ void " << bounds << " pcgb_search_c" << c
@@ -811,7 +822,7 @@ static int lm_run_impl(pcgb_fitter* ft, const void* consts, int64_t consts_strid
   prm.bstride = bounds_stride;
   prm.iters = iters;
   prm.flags = flags;
-  if (fresh) prm.lam0 = lam0;
+  if (fresh) prm.lam_start = lam0;
   set_lm_constants(prm, tol, mu, eta, acc, dec);
   const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_LM_C1_B1 : K_LM_C1_B0)
                                              : (bounds_stride == 0 ? K_LM_C0_B1 : K_LM_C0_B0);
@@ -969,13 +980,13 @@ int pcgb_lm_run_select(pcgb_fitter* ft, const void* consts, int64_t consts_strid
                      protocol_len, lb_host, ub_host, block, nullptr, 0, stream, nullptr, 0, nullptr, &fb);
 }
 
-int pcgb_warm_check(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
-                    const void* lower_bound, const void* upper_bound, int64_t bounds_stride,
-                    const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
-                    const double* init_values, double lam0, void* params, void* lam, int8_t* step_type, void* f,
-                    void* cost, void* pars_backup, void* cost_backup, int32_t* fb_idx, uint32_t* fb_count,
-                    int64_t nprobs, void* stream) {
-  g_err.clear();
+// Launch parameters of a fallback check (pcgb_warm_check, pcgb_warm_lm_check).
+static int check_params(pcgb_fitter* ft, PcgbLmParams& prm, const void* consts, int64_t consts_stride,
+                        const void* data, const void* lower_bound, const void* upper_bound, int64_t bounds_stride,
+                        const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                        const double* init_values, double lam0, void* params, void* lam, int8_t* step_type, void* f,
+                        void* cost, void* pars_backup, void* cost_backup, int32_t* fb_idx, uint32_t* fb_count,
+                        int64_t nprobs) {
   if (!ft) return fail(PCGB_EINVAL, "fitter is NULL");
   if (nprobs < 0) return fail(PCGB_EINVAL, "nprobs must be >= 0");
   if (nprobs > (int64_t(1) << 31) - 1) return fail(PCGB_ERANGE, "warm check indexes voxels with int32");
@@ -983,7 +994,6 @@ int pcgb_warm_check(pcgb_fitter* ft, const void* consts, int64_t consts_stride, 
   if (nprobs > 0 && (!data || !params || !lam || !step_type || !f || !cost || !pars_backup || !cost_backup || !fb_idx))
     return fail(PCGB_EINVAL, "data, params, lam, step_type, f, cost, backups and fb_idx are required");
   if (int rc = check_device(ft)) return rc;
-  PcgbLmParams prm;
   std::memset(&prm, 0, sizeof(prm));
   if (int rc = fill_protocol(ft, prm, consts_stride, nprobs, protocol_host, protocol_len)) return rc;
   if (consts_stride != 0 && !consts) return fail(PCGB_EINVAL, "per-voxel consts pointer is NULL");
@@ -1015,10 +1025,53 @@ int pcgb_warm_check(pcgb_fitter* ft, const void* consts, int64_t consts_stride, 
   prm.fb_count = fb_count;
   prm.lam0 = lam0;
   prm.N = nprobs;
+  prm.n_items = nprobs;
+  return PCGB_OK;
+}
+
+int pcgb_warm_check(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                    const void* lower_bound, const void* upper_bound, int64_t bounds_stride,
+                    const double* protocol_host, int protocol_len, const double* lb_host, const double* ub_host,
+                    const double* init_values, double lam0, void* params, void* lam, int8_t* step_type, void* f,
+                    void* cost, void* pars_backup, void* cost_backup, int32_t* fb_idx, uint32_t* fb_count,
+                    int64_t nprobs, void* stream) {
+  g_err.clear();
+  PcgbLmParams prm;
+  if (int rc = check_params(ft, prm, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride,
+                            protocol_host, protocol_len, lb_host, ub_host, init_values, lam0, params, lam, step_type,
+                            f, cost, pars_backup, cost_backup, fb_idx, fb_count, nprobs))
+    return rc;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemsetAsync(fb_count, 0, 2 * sizeof(uint32_t), st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
   return launch(ft, consts_stride == 0 ? K_CHECK_C1 : K_CHECK_C0, prm, nprobs, 256, stream);
+}
+
+int pcgb_warm_lm_check(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,
+                       const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
+                       double eta, double acc, double dec, int iters, double lam_start, const double* protocol_host,
+                       int protocol_len, const double* lb_host, const double* ub_host, const double* init_values,
+                       double lam0, void* params, void* lam, int8_t* step_type, void* f, void* cost,
+                       void* pars_backup, void* cost_backup, int32_t* fb_idx, uint32_t* fb_count, int64_t nprobs,
+                       int block, void* stream) {
+  g_err.clear();
+  if (iters < 0) return fail(PCGB_EINVAL, "iters must be >= 0");
+  if (!(lam_start > 0.0)) return fail(PCGB_EINVAL, "lam_start must be > 0");
+  PcgbLmParams prm;
+  if (int rc = check_params(ft, prm, consts, consts_stride, data, lower_bound, upper_bound, bounds_stride,
+                            protocol_host, protocol_len, lb_host, ub_host, init_values, lam0, params, lam, step_type,
+                            f, cost, pars_backup, cost_backup, fb_idx, fb_count, nprobs))
+    return rc;
+  prm.iters = iters;
+  prm.flags = PCGB_LM_FRESH | PCGB_LM_PARS_ONLY;
+  prm.lam_start = lam_start;
+  set_lm_constants(prm, tol, mu, eta, acc, dec);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMemsetAsync(fb_count, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");
+  const KernelSlot slot = consts_stride == 0 ? (bounds_stride == 0 ? K_LMW_C1_B1 : K_LMW_C1_B0)
+                                             : (bounds_stride == 0 ? K_LMW_C0_B1 : K_LMW_C0_B0);
+  return launch(ft, slot, prm, nprobs, block, stream);
 }
 
 int pcgb_warm_select(pcgb_fitter* ft, const void* consts, int64_t consts_stride, const void* data,

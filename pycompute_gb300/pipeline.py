@@ -239,6 +239,20 @@ class WarmStartFitter:
             _p(b["idx"]), _p(b["counts"]), data.shape[1], _stream())
         _lib.check("pcgb_warm_check", rc)
 
+    def _warm_lm_check(self, solm, data, pars, b, iters_warm, lam0, tol=1e-8, mu=0.25, eta=0.75, acc=0.2, dec=2.0):
+        """The warm LM from a fresh start with the fallback check as its
+        epilogue (pcgb_warm_lm_check)."""
+        w = self.w
+        pv, plen = solm._proto_args()
+        rc = _lib.lib().pcgb_warm_lm_check(
+            solm.build().handle, _p(solm.consts_t), solm._cstride, _p(data), _p(solm.lower_bound_t),
+            _p(solm.upper_bound_t), solm._bstride, float(tol), float(mu), float(eta), float(acc), float(dec),
+            int(iters_warm), float(lam0), pv, plen, _dvec(solm._lb_host) if solm._bstride == 0 else None,
+            _dvec(solm._ub_host) if solm._bstride == 0 else None, _dvec(w.init_values), 5.0, _p(pars),
+            _p(solm.lam_t), _p(solm.step_type_t), _p(solm.f_t), _p(b["cost"]), _p(b["backup"]), _p(b["cost_b"]),
+            _p(b["idx"]), _p(b["counts"]), data.shape[1], 0, _stream())
+        _lib.check("pcgb_warm_lm_check", rc)
+
     def _buffers(self, P: int, N: int, dev):
         key = (P, N, str(dev))
         if getattr(self, "_buf_key", None) != key:
@@ -260,6 +274,11 @@ class WarmStartFitter:
 
         ``fused="select"`` (default) runs the fallback check as its own kernel
         and the select as the epilogue of the refit launch;
+        ``fused="lean"`` runs the warm LM and the check as one kernel (the
+        warm fit's cost taken from the iterations instead of re-evaluated; the
+        same rule, its cost comparisons on costs rounded differently, so a
+        voxel whose two costs tie to rounding may be flagged differently) and
+        the select as the refit's epilogue;
         ``fused="epilogue"`` also runs the check as the epilogue of the warm
         LM launch (the signals are read once, but the LM kernel then holds
         more registers); ``fused=True`` runs check, refit and select as three
@@ -290,7 +309,7 @@ class WarmStartFitter:
         pars = self.net.infer(data, out=pars_out)
         mark("network")
         solm = self._fitter()
-        if fused == "select":
+        if fused in ("select", "lean"):
             # the warm LM reads no state and keeps only the parameters and step
             # codes; the check initialises the state of the voxels it flags
             solm.setup(pars, prot, data, lb, ub, init_state=False)
@@ -298,9 +317,13 @@ class WarmStartFitter:
             solm.setup(pars, prot, data, lb, ub)
             solm.lam_t.fill_(lam0)
         mark("setup")
-        if fused in ("epilogue", "select"):
+        if fused in ("epilogue", "select", "lean"):
             b = self._buffers(P, N, dev)
-            if fused == "epilogue":  # the check as the warm LM's epilogue
+            if fused == "lean":  # fresh warm LM with the check as its epilogue
+                self._warm_lm_check(solm, data, pars, b, iters_warm, lam0)
+                mark("lm_warm")
+                mark("check")
+            elif fused == "epilogue":  # the check as the warm LM's epilogue
                 solm.run_check(iters_warm, w.init_values, 5.0, b["cost"], b["backup"], b["cost_b"], b["idx"],
                                b["counts"])
                 mark("lm_warm")

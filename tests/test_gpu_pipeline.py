@@ -113,6 +113,54 @@ def test_fused_fallback_matches_separate_kernels(per_voxel_bounds, schedule, mod
     np.testing.assert_array_equal(c0, c1)
 
 
+@pytest.mark.parametrize("per_voxel_bounds", [False, True])
+def test_lean_warm_lm_with_check_epilogue_matches_select_pipeline(per_voxel_bounds):
+    """The warm LM from a fresh start with the check as its epilogue
+    (fused="lean") against the pipeline with the check as its own kernel
+    (fused="select"): the same warm iterations and rule, but the warm fit's cost
+    comes from the iterations instead of a second evaluation, so the two costs
+    a decision compares differ by rounding. The flagged sets may differ only on
+    voxels whose warm cost and constant-start cost tie to 1e-5; voxels flagged
+    by neither end bit-equal; voxels flagged by both end equal unless the
+    select compared a tie (final costs within 1e-5)."""
+    w = synth.ivim(synth.ivim_b16(), name="ivim16")
+    _, data = pipeline.synth_gpu(w, 50001, seed=17, device=DEV)
+    N = data.shape[1]
+    lbt = torch.tensor(w.lb, device=DEV)[:, None].expand(w.P, N).contiguous()
+    ubt = torch.tensor(w.ub, device=DEV)[:, None].expand(w.P, N).contiguous()
+    out = []
+    for fused in ("select", "lean"):
+        wf = pipeline.WarmStartFitter(w, _BadNet(w))
+        if per_voxel_bounds:
+            wf._consts = lambda dev: (list(w.protocol), lbt, ubt)
+        res = wf.fit(data, iters_warm=3, iters_fallback=20, fused=fused)
+        torch.cuda.synchronize()
+        flagged = np.zeros(N, dtype=bool)
+        flagged[res.fallback_idx[:res.n_fallback].cpu().numpy()] = True
+        out.append((res.pars.cpu().numpy().copy(), res.cost.cpu().numpy().copy(), flagged))
+    (p0, c0, f0), (p1, c1, f1) = out
+    assert f0.sum() >= 16667
+    # the warm fit and its two costs, evaluated as the separate check does
+    wf = pipeline.WarmStartFitter(w, _BadNet(w))
+    warm = wf.net.infer(data)
+    solm = wf._fitter()
+    solm.setup(warm, list(w.protocol), data, list(w.lb), list(w.ub))
+    solm.run_fresh(3, 1e-3)
+    cw = solm.cost().cpu().numpy().astype(np.float64)
+    cs = solm.cost(pipeline.init_constant(data, w.init_values)).cpu().numpy().astype(np.float64)
+    torch.cuda.synchronize()
+    differ = f0 != f1
+    assert differ.mean() <= 1e-3, differ.mean()
+    assert np.all(np.abs(cw[differ] - cs[differ]) <= 1e-5 * cs[differ]), np.where(differ)[0][:10]
+    neither = ~f0 & ~f1
+    np.testing.assert_array_equal(p0[:, neither], p1[:, neither])
+    np.testing.assert_allclose(c1[neither], c0[neither], rtol=1e-5)
+    both = f0 & f1
+    same = np.all(p0 == p1, axis=0)
+    assert (both & ~same).sum() <= 1e-3 * both.sum() + 1
+    np.testing.assert_allclose(c1[both], c0[both], rtol=1e-5)
+
+
 def test_fallback_flags_match_the_rule_on_the_oracle():
     """The fused check's flagged set against the fallback rule evaluated on the
     CPU by the oracle, on the same warm fits: a voxel is flagged when its cost
