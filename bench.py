@@ -480,6 +480,23 @@ def fallback_rule_report(run_warm, run_pre, run_plain, plain, k_warm, k_plain, r
             out[f"voxels_above_plain_{name}"] = {"voxels": int(big.sum()), "warm_median_rel_err": ew[0],
                                                  "warm_frac_gt_1e-4": ew[1], "plain_median_rel_err": ep[0],
                                                  "plain_frac_gt_1e-4": ep[1]}
+    # candidate proxies for "the warm fit ends above the plain fit's cost":
+    # the last warm iteration still lowered the cost by more than delta
+    # (relative); newly flagged voxels would be refitted and keep the lower
+    # cost of the two fits (the select), which is evaluated here directly
+    if k_warm >= 1:
+        _, c_prev, _ = run_pre(k_warm - 1) if k_warm > 1 else (None, const_cost, None)
+        target = unflagged & (w_cost > c_pl * (1.0 + 1e-4))
+        prox = {}
+        for delta in (1e-2, 1e-3, 1e-4, 1e-5):
+            extra = unflagged & ((c_prev - pre_cost) > delta * pre_cost)
+            take = extra & (c_pl < w_cost)
+            med_x, frac_x = _median_rel_gpu(torch.where(take[None], p_pl, w_pars), ref)
+            prox[f"last_iter_drop_gt_{delta:g}"] = {
+                "extra_flagged": int(extra.sum()), "extra_flagged_frac": float(extra.double().mean()),
+                "recall_of_above_plain_rel_1e-4": float((extra & target).sum()) / max(1, int(target.sum())),
+                "accuracy_if_refitted": {"median_rel_err": med_x, "frac_voxels_gt_1e-4": frac_x}}
+        out["proxies"] = prox
     del p_pl, ideal, pre_pars
     return out
 
@@ -769,7 +786,7 @@ def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
     t0 = time.perf_counter()
     tuned = autotune(models, lambda: make_jobs(0.125), iters=20)
     tune_s = time.perf_counter() - t0
-    fitter = MultiModelFitter(models, block=tuned["block"], maxrreg=tuned["maxrreg"])
+    fitter = MultiModelFitter(models, block=tuned["block"], maxrreg=tuned["maxrreg"], lanes=tuned.get("lanes"))
     fitter.chunk = tuned["chunk"]
     fitter.order = tuned.get("order")
     jobs = make_jobs()
@@ -820,9 +837,24 @@ def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
         med, frac = _median_rel_gpu(j.pars, p64)
         acc[w.name] = {"median_rel_err": med, "frac_voxels_gt_1e-4": frac,
                        "per_param_median": _per_param_median(j.pars, p64)}
-        del s64, p64
+        # the model's own 1e-4 budget: error against the converged all-FP64
+        # fit (300 iterations, tol 1e-30) of the fp32 fitter at growing budgets
+        s64.setup(p64.copy_(i0.double()), list(w.protocol), j.data.double(), list(w.lb), list(w.ub))
+        s64.run(300, tol=1e-30)
+        s32 = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float32)
+        curve, k_tol = {}, None
+        for k in (25, 50, 100, 200, 400):
+            p32 = i0.clone()
+            s32.setup(p32, list(w.protocol), j.data, list(w.lb), list(w.ub))
+            s32.run(k)
+            curve[k] = _median_rel_gpu(p32, p64)[0]
+            if k_tol is None and curve[k] <= TOL:
+                k_tol = k
+        acc[w.name]["vs_fp64_converged"] = {"median_rel_err_by_iters": curve, "iters_for_1e-4": k_tol}
+        del s64, p64, s32
     return {"workload": "mixed_vfa8_t2s16_ivim10_biexp32", "voxels": total, "iters": iters,
-            "autotuned": {k: tuned.get(k) for k in ("block", "maxrreg", "chunk", "order", "ms")},
+            "autotuned": {k: tuned.get(k) for k in ("block", "maxrreg", "chunk", "order", "lanes", "ms")},
+            "lanes_per_voxel_trials": tuned.get("lane_trials"),
             "tune_s": round(tune_s, 1),
             "one_launch_fits_per_s": total / (ms_multi / 1e3), "graph_fits_per_s": total / (ms_graph / 1e3),
             "per_model_launches_fits_per_s": total / (ms_single / 1e3), "mean_iters_per_model": its,

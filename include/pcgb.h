@@ -327,10 +327,13 @@ typedef struct {
 } pcgb_multi_job;
 
 /* Compile one program for n_models models (NVRTC, sm_103a, disk cache).
- * maxrreg: register cap (0 = compiler's choice); block: threads per block. */
+ * maxrreg: register cap (0 = compiler's choice); block: threads per block;
+ * lanes (may be NULL = all 1): per model, the warp lanes that share one
+ * voxel (1 or 2; with 2 the two lanes split the voxel's samples and sum
+ * their shares, so results match one lane's to float rounding). */
 int pcgb_multi_create(int n_models, const char* const* model_sources, const char* const* model_structs,
                       const int* nparam, const int* nconst, const int* ndata, int dtype, int solve_dtype, int maxrreg,
-                      int block, const char* cache_dir, pcgb_multi** out);
+                      int block, const int* lanes, const char* cache_dir, pcgb_multi** out);
 int pcgb_multi_destroy(pcgb_multi* program);
 const char* pcgb_multi_log(const pcgb_multi* program);
 /* Persistent grid size: resident blocks per SM x SMs. */
@@ -475,6 +478,19 @@ int pcgb_gemm_bf16(int a_layout, int b_layout, int epilogue, const void* A, int6
                    int64_t M, int64_t N, int64_t K, int64_t k_split, const float* bias, int64_t bias_stride,
                    float* out_f32, int64_t ldo, void* out_bf16, int64_t ldob, const float* zin, int64_t ldz,
                    void* stream);
+
+/* pcgb_gemm_bf16 on the 5th-generation tensor cores (tcgen05.mma, fp32
+ * accumulator in tensor memory; no reference counterpart): same arguments,
+ * layouts, epilogues and results up to fp32 summation order. status (device
+ * int, may be NULL) is set to 1 if a CTA gave up on a bounded wait for its
+ * tensor-core work (its tile of the output is then not written). */
+int pcgb_gemm_bf16_tc(int a_layout, int b_layout, int epilogue, const void* A, int64_t lda, const void* B,
+                      int64_t ldb, int64_t M, int64_t N, int64_t K, int64_t k_split, const float* bias,
+                      int64_t bias_stride, float* out_f32, int64_t ldo, void* out_bf16, int64_t ldob,
+                      const float* zin, int64_t ldz, int* status, void* stream);
+
+/* Last error of pcgb_gemm_bf16_tc on this host thread. */
+const char* pcgb_gemm_tc_last_error(void);
 
 /* Mean-squared-error gradient dy = 2 (y - t) / (batch * nout) (bf16, zero in
  * padding columns nout..ncols-1) and loss_sum += mean squared error. */

@@ -75,7 +75,7 @@ SIGNATURES = {
                                    c_void_p, c_i64, c_int, c_int, c_double, c_double, c_double, c_double, c_double,
                                    ctypes.c_uint64, c_void_p, c_int, c_void_p, c_void_p, c_void_p]),
     "pcgb_multi_create": (c_int, [c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int, c_int, c_int, c_int,
-                                  c_char_p, ctypes.POINTER(c_void_p)]),
+                                  c_void_p, c_char_p, ctypes.POINTER(c_void_p)]),
     "pcgb_multi_destroy": (c_int, [c_void_p]),
     "pcgb_multi_log": (c_char_p, [c_void_p]),
     "pcgb_multi_grid": (c_int, [c_void_p]),
@@ -102,6 +102,10 @@ SIGNATURES = {
     "pcgb_mlp_last_error": (c_char_p, []),
     "pcgb_gemm_bf16": (c_int, [c_int, c_int, c_int, c_void_p, c_i64, c_void_p, c_i64, c_i64, c_i64, c_i64, c_i64,
                                c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p]),
+    "pcgb_gemm_bf16_tc": (c_int, [c_int, c_int, c_int, c_void_p, c_i64, c_void_p, c_i64, c_i64, c_i64, c_i64,
+                                  c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p,
+                                  c_void_p]),
+    "pcgb_gemm_tc_last_error": (c_char_p, []),
     "pcgb_mlp_mse_grad": (c_int, [c_void_p, c_void_p, c_i64, c_i64, c_int, c_int, c_void_p, c_i64, c_void_p,
                                   c_void_p]),
     "pcgb_adam_step": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_i64, c_i64, c_i64, ctypes.c_float,
@@ -151,7 +155,9 @@ def lib(build_if_missing: bool = True):
 def check(fn_name: str, rc: int):
     if rc != 0:
         L = lib()
-        if fn_name.startswith("pcgb_mlp_forward_tc"):  # also pcgb_mlp_forward_tc_ex
+        if fn_name.startswith("pcgb_gemm_bf16_tc"):
+            err = L.pcgb_gemm_tc_last_error
+        elif fn_name.startswith("pcgb_mlp_forward_tc"):  # also pcgb_mlp_forward_tc_ex
             err = L.pcgb_mlp_tc_last_error
         elif fn_name.startswith(("pcgb_gemm", "pcgb_mlp", "pcgb_adam")):
             err = L.pcgb_mlp_last_error

@@ -1,0 +1,292 @@
+// Training GEMMs of the warm-start network on the 5th-generation tensor cores.
+//
+// C(M x N) = A(M x K) * B(K x N) with bf16 operands and an fp32 accumulator in
+// tensor memory, with the epilogues of the training step fused (bias + GELU
+// storing the pre-activation and the bf16 activation, bias only, GELU' times
+// the incoming gradient, split-K accumulation of weight gradients with
+// atomics, plain fp32 store). Same arguments, layouts and results (up to fp32
+// summation order) as the warp-level mma.sync GEMM of mlp.cu:
+//   a_layout 0: A stored (M, K) row-major (K-major), 1: (K, M) row-major
+//   b_layout 0: B stored (N, K) row-major (K-major), 1: (K, N) row-major
+//
+// One CTA of 128 threads computes a 128 x 64 tile of C over its K range
+// (blockIdx.z selects the split-K range). Per 32-wide K step the threads stage
+// both operand tiles into shared memory in the canonical K-major core-matrix
+// layout (a transposed operand is scattered element by element while staging,
+// so every MMA reads the layout the inference kernel uses), and one thread
+// issues two tcgen05.mma (M = 128, N = 64, K = 16) into the 64 accumulator
+// columns and commits them to the stage's mbarrier; two stages alternate, so
+// staging step t + 1 overlaps the MMAs of step t. The epilogue reads row r of
+// the accumulator (thread r = TMEM lane r) with tcgen05.ld. Every mbarrier
+// wait is bounded: on timeout the CTA records the loss in *status, waits once
+// more (bounded) for its MMAs in flight, skips its epilogue and still frees
+// its tensor memory.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+
+#include "mlp_math.cuh"
+#include "pcgb.h"
+#include "tc_common.cuh"
+
+namespace pcgb_gemm_tc {
+
+using pcgb_mlp::bf16;
+using namespace pcgb_tc;
+
+constexpr int BM = 128, BN = 64, BK = 32;
+constexpr int THREADS = 128;
+constexpr int TMEM_COLS = 64;
+constexpr unsigned kWaitLimit = 1u << 22;
+// dynamic shared memory requested per CTA: at most 7 CTAs fit on an SM, so
+// their 7 x 64 accumulator columns never exceed the SM's 512 and no
+// tcgen05.alloc has to wait for another CTA
+constexpr int kSmemBytes = 32 * 1024;
+
+enum Epilogue { EPI_FWD_GELU = 0, EPI_FWD_LINEAR = 1, EPI_BWD_DGELU = 2, EPI_DW_ATOMIC = 3, EPI_STORE_F32 = 4 };
+
+struct TcGemmArgs {
+  const bf16* A;
+  long long lda;
+  const bf16* B;
+  long long ldb;
+  long long M, N, K;
+  long long k_split;
+  const float* bias;
+  long long bias_stride;
+  float* out_f32;
+  long long ldo;
+  bf16* out_bf16;
+  long long ldob;
+  const float* zin;
+  long long ldz;
+  int* status;
+};
+
+struct __align__(1024) GemmSmem {
+  bf16 a[2][BM * BK];
+  bf16 b[2][BN * BK];
+  unsigned long long mbar[2];
+  uint32_t tmem_base;
+};
+static_assert(sizeof(GemmSmem) <= kSmemBytes && kSmemBytes <= 48 * 1024, "GEMM shared memory");
+
+// Stage the rows x BK tile at (r0, k0) of an operand into the canonical
+// K-major layout. KMAJOR: element (r, k) at src[r * ld + k], else at
+// src[k * ld + r]. Rows >= rows_live are loaded when the stored row is long
+// enough (their results are masked); columns at or past kend are zero.
+template <int ROWS, bool KMAJOR>
+__device__ __forceinline__ void stage(bf16* dst, const bf16* src, long long ld, long long r0, long long rows_live,
+                                      long long k0, long long kend) {
+  unsigned char* base = reinterpret_cast<unsigned char*>(dst);
+  if (KMAJOR) {
+    // ROWS x (BK / 8) chunks of 8 k-values
+    for (int c = threadIdx.x; c < ROWS * (BK / 8); c += THREADS) {
+      const int r = c / (BK / 8), kc = (c % (BK / 8)) * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (r0 + r < rows_live && k0 + kc < kend) v = *reinterpret_cast<const uint4*>(src + (r0 + r) * ld + k0 + kc);
+      *reinterpret_cast<uint4*>(base + core_off(r, kc, BK)) = v;
+    }
+  } else {
+    // BK x (ROWS / 8) chunks of 8 row-values, scattered into their rows
+    for (int c = threadIdx.x; c < BK * (ROWS / 8); c += THREADS) {
+      const int kr = c / (ROWS / 8), rc = (c % (ROWS / 8)) * 8;
+      uint4 v = make_uint4(0, 0, 0, 0);
+      if (r0 + rc < rows_live && k0 + kr < kend) v = *reinterpret_cast<const uint4*>(src + (k0 + kr) * ld + r0 + rc);
+      const unsigned short* e = reinterpret_cast<const unsigned short*>(&v);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) *reinterpret_cast<unsigned short*>(base + core_off(rc + q, kr, BK)) = e[q];
+    }
+  }
+}
+
+template <bool A_ROW, bool B_NK, int EPI>
+__global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  GemmSmem& S = *reinterpret_cast<GemmSmem*>(smem_raw);
+  const int warp = threadIdx.x >> 5;
+  const long long m0 = (long long)blockIdx.y * BM, n0 = (long long)blockIdx.x * BN;
+  const long long kbeg = (long long)blockIdx.z * g.k_split;
+  const long long kend = kbeg + g.k_split < g.K ? kbeg + g.k_split : g.K;
+  const int steps = int((kend - kbeg + BK - 1) / BK);
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < 2; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.mbar[i])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&S.tmem_base)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_before_sync();
+  __syncthreads();
+  fence_after_sync();
+  const uint32_t tbase = S.tmem_base;
+  constexpr uint32_t ID = idesc_bf16(BM, BN);
+  bool lost = false;
+
+  for (int t = 0; t < steps; ++t) {
+    const int buf = t & 1;
+    // the MMAs of step t - 2 read this buffer: wait for their commit
+    if (t >= 2) {
+      const bool ok = threadIdx.x != 0 || mbar_wait(smem_u32(&S.mbar[buf]), uint32_t(((t - 2) >> 1) & 1), kWaitLimit);
+      if (__syncthreads_or(!ok)) {
+        lost = true;
+        break;
+      }
+    }
+    const long long k0 = kbeg + (long long)t * BK;
+    stage<BM, A_ROW>(S.a[buf], g.A, g.lda, m0, g.M, k0, kend);
+    stage<BN, B_NK>(S.b[buf], g.B, g.ldb, n0, g.N, k0, kend);
+    fence_async_smem();  // staged operands -> visible to the tensor cores
+    fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      fence_after_sync();
+      const uint32_t as = smem_u32(S.a[buf]), bs = smem_u32(S.b[buf]);
+#pragma unroll
+      for (int kk = 0; kk < BK / 16; ++kk)
+        mma_bf16(tbase, smem_desc(as + kk * 256, 128, (BK / 8) * 128), smem_desc(bs + kk * 256, 128, (BK / 8) * 128),
+                 ID, (t > 0 || kk > 0) ? 1u : 0u);
+      mma_commit(smem_u32(&S.mbar[buf]));
+    }
+  }
+  // the last commit covers every MMA of this CTA
+  if (!lost && steps > 0) {
+    const int last = steps - 1;
+    const bool ok = threadIdx.x != 0 ||
+                    mbar_wait(smem_u32(&S.mbar[last & 1]), uint32_t((last >> 1) & 1), kWaitLimit);
+    lost = __syncthreads_or(!ok);
+  }
+  if (lost) {
+    if (threadIdx.x == 0) {
+      // MMAs of the lost phase may still complete: wait for them (bounded)
+      // before the tensor memory they write is returned
+      for (int b = 0; b < 2; ++b) (void)mbar_wait(smem_u32(&S.mbar[b]), 0u, kWaitLimit);
+      if (g.status) atomicExch(g.status, 1);
+    }
+  } else {
+    fence_after_sync();
+    const int r = threadIdx.x;  // accumulator row = TMEM lane
+    const long long m = m0 + r;
+    const uint32_t trow = tbase + (uint32_t(warp * 32) << 16);
+#pragma unroll
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      float v[16];
+      if (steps > 0) {
+        tmem_ld16(trow + uint32_t(c0), v);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) v[i] = 0.f;
+      }
+      if (m >= g.M) continue;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const long long n = n0 + c0 + i;
+        if (n >= g.N) break;
+        const float acc = v[i];
+        if (EPI == EPI_FWD_GELU) {
+          const float z = acc + g.bias[n * g.bias_stride];
+          g.out_f32[m * g.ldo + n] = z;
+          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(pcgb_mlp::gelu(z));
+        } else if (EPI == EPI_FWD_LINEAR) {
+          g.out_f32[m * g.ldo + n] = acc + g.bias[n * g.bias_stride];
+        } else if (EPI == EPI_BWD_DGELU) {
+          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(acc * pcgb_mlp::gelu_grad(g.zin[m * g.ldz + n]));
+        } else if (EPI == EPI_DW_ATOMIC) {
+          atomicAdd(&g.out_f32[m * g.ldo + n], acc);
+        } else {
+          g.out_f32[m * g.ldo + n] = acc;
+        }
+      }
+    }
+  }
+  fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    fence_after_sync();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+template <bool A_ROW, bool B_NK>
+cudaError_t launch_tc(int epi, const TcGemmArgs& g, dim3 grid, cudaStream_t s) {
+  // kSmemBytes is below the 48 KB a launch may request without opting in, so
+  // no function attribute is set (the training step is captured in a graph)
+  auto pick = [&](auto kern) {
+    kern<<<grid, THREADS, kSmemBytes, s>>>(g);
+    return cudaGetLastError();
+  };
+  switch (epi) {
+    case EPI_FWD_GELU: return pick(gemm_tc_kernel<A_ROW, B_NK, EPI_FWD_GELU>);
+    case EPI_FWD_LINEAR: return pick(gemm_tc_kernel<A_ROW, B_NK, EPI_FWD_LINEAR>);
+    case EPI_BWD_DGELU: return pick(gemm_tc_kernel<A_ROW, B_NK, EPI_BWD_DGELU>);
+    case EPI_DW_ATOMIC: return pick(gemm_tc_kernel<A_ROW, B_NK, EPI_DW_ATOMIC>);
+    default: return pick(gemm_tc_kernel<A_ROW, B_NK, EPI_STORE_F32>);
+  }
+}
+
+thread_local std::string g_err;
+
+int fail(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
+
+}  // namespace pcgb_gemm_tc
+
+using namespace pcgb_gemm_tc;
+
+extern "C" {
+
+const char* pcgb_gemm_tc_last_error(void) { return g_err.c_str(); }
+
+int pcgb_gemm_bf16_tc(int a_layout, int b_layout, int epilogue, const void* A, int64_t lda, const void* B,
+                      int64_t ldb, int64_t M, int64_t N, int64_t K, int64_t k_split, const float* bias,
+                      int64_t bias_stride, float* out_f32, int64_t ldo, void* out_bf16, int64_t ldob,
+                      const float* zin, int64_t ldz, int* status, void* stream) {
+  g_err.clear();
+  if (M < 0 || N < 0 || K < 0) return fail(PCGB_EINVAL, "negative GEMM size");
+  if (K % 8 || lda % 8 || ldb % 8) return fail(PCGB_EINVAL, "K, lda and ldb must be multiples of 8");
+  if (epilogue < 0 || epilogue > 4) return fail(PCGB_EINVAL, "unknown epilogue");
+  if (!A || !B) return fail(PCGB_EINVAL, "A and B are required");
+  // every 16-byte operand chunk a tile reads must lie inside the stored rows:
+  // a transposed operand is read in chunks of 8 rows up to the tile's row
+  // count rounded to 8
+  const int64_t m8 = (M + 7) / 8 * 8, n8 = (N + 7) / 8 * 8;
+  if ((a_layout == 0 && lda < K) || (a_layout != 0 && lda < m8) || (b_layout == 0 && ldb < K) ||
+      (b_layout != 0 && ldb < n8))
+    return fail(PCGB_EINVAL, "leading dimension smaller than the stored row");
+  const bool need_bias = epilogue == EPI_FWD_GELU || epilogue == EPI_FWD_LINEAR;
+  if (!out_f32 && epilogue != EPI_BWD_DGELU) return fail(PCGB_EINVAL, "out_f32 is required");
+  if ((epilogue == EPI_FWD_GELU || epilogue == EPI_BWD_DGELU) && !out_bf16)
+    return fail(PCGB_EINVAL, "out_bf16 is required");
+  if (need_bias && !bias) return fail(PCGB_EINVAL, "bias is required");
+  if (epilogue == EPI_BWD_DGELU && !zin) return fail(PCGB_EINVAL, "zin is required");
+  if (M == 0 || N == 0) return PCGB_OK;
+  if (k_split <= 0 || k_split >= K) k_split = K;
+  else if (k_split % BK) k_split = (k_split + BK - 1) / BK * BK;
+  if (k_split > K) k_split = K;
+  if (k_split != K && epilogue != EPI_DW_ATOMIC) return fail(PCGB_EINVAL, "split-K needs the atomic epilogue");
+  const long long splits = K == 0 ? 1 : (K + k_split - 1) / k_split;
+  if ((N + BN - 1) / BN > 0x7fffffffLL || (M + BM - 1) / BM > 65535 || splits > 65535)
+    return fail(PCGB_ERANGE, "GEMM grid too large");
+  TcGemmArgs g{static_cast<const bf16*>(A), lda, static_cast<const bf16*>(B), ldb, M, N, K, k_split,
+               bias, bias_stride, out_f32, ldo, static_cast<bf16*>(out_bf16), ldob, zin, ldz, status};
+  dim3 grid(unsigned((N + BN - 1) / BN), unsigned((M + BM - 1) / BM), unsigned(splits));
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (a_layout == 0 && b_layout == 0) e = launch_tc<true, true>(epilogue, g, grid, s);
+  else if (a_layout == 0) e = launch_tc<true, false>(epilogue, g, grid, s);
+  else if (b_layout == 0) e = launch_tc<false, true>(epilogue, g, grid, s);
+  else e = launch_tc<false, false>(epilogue, g, grid, s);
+  if (e != cudaSuccess) return fail(PCGB_ECUDA, cudaGetErrorString(e));
+  return PCGB_OK;
+}
+
+}  // extern "C"

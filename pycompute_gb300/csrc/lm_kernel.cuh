@@ -413,11 +413,29 @@ constexpr int sample_unroll() { return SameType<TA, float>::value && SameType<TS
 // the last iterate when its step was rejected or the voxel converged, the
 // trial cost when the step was accepted and no bound moved the point), NaN
 // otherwise.
-template <class Model, int M, typename TA, typename TS, class CF>
-PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const TA (&lo)[Model::P],
-                        const TA (&hi)[Model::P], TA (&stp)[Model::P], TA& lam, int& st, TA& f, TA& first, int& done,
-                        int iters, TA tol, TA mu, TA eta, TA acc, TA dec, TA& fend) {
-  constexpr int P = Model::P, H = Model::H, C = Model::C;
+//
+// LANES > 1 splits a voxel's samples over LANES adjacent lanes of the warp
+// (lane `sub` takes samples sub, sub + LANES, ...; d holds those): each lane
+// accumulates its share of f, g, h and of the trial cost, the shares are
+// summed across the lanes, and every lane then runs the same solve and
+// decisions on the same sums (addition is commutative, so the lanes agree
+// bit for bit). Only LANES = 1 and 2 are supported.
+template <int M, int LANES> constexpr int lane_samples() { return (M + LANES - 1) / LANES; }
+template <int LANES, typename T> PCGB_HD T lane_sum(T x) {
+  if constexpr (LANES == 2) {
+    const unsigned pair = 3u << ((threadIdx.x & 31u) & ~1u);
+    x += __shfl_xor_sync(pair, x, 1);
+  }
+  return x;
+}
+
+template <class Model, int M, typename TA, typename TS, int LANES = 1, class CF>
+PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[lane_samples<M, LANES>()], TA (&p)[Model::P],
+                        const TA (&lo)[Model::P], const TA (&hi)[Model::P], TA (&stp)[Model::P], TA& lam, int& st,
+                        TA& f, TA& first, int& done, int iters, TA tol, TA mu, TA eta, TA acc, TA dec, TA& fend,
+                        int sub = 0) {
+  static_assert(LANES == 1 || LANES == 2, "one or two lanes per voxel");
+  constexpr int P = Model::P, H = Model::H, C = Model::C, ML = lane_samples<M, LANES>();
   fend = Num<TA>::nan();
   for (int it = 0; it < iters; ++it) {
     if (st == 0) break;
@@ -434,11 +452,13 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
     // 30.3 -> 28.3 ms; the samples then sit in L1-cached local memory),
     // unrolled where instruction issue bounds it (fp32 solve: IVIM-10, 1 M
     // voxels x 20 iterations 1.21 ms unrolled, 1.45 ms rolled).
-#pragma unroll (sample_unroll<TA, TS, M>())
-    for (int i = 0; i < M; ++i) {
+#pragma unroll (sample_unroll<TA, TS, ML>())
+    for (int i = 0; i < ML; ++i) {
+      const int smp = i * LANES + sub;
+      if (LANES > 1 && smp >= M) break;
       TA c[C > 0 ? C : 1];
 #pragma unroll
-      for (int k = 0; k < C; ++k) c[k] = cf(k, i);
+      for (int k = 0; k < C; ++k) c[k] = cf(k, smp);
       TA m, J[P], Hm[H];
       Model::template all<TA>(p, c, m, J, Hm);
       const TA r = m - d[i];
@@ -454,6 +474,16 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
         }
         g[j] += J[j] * r;
       }
+    }
+    if constexpr (LANES > 1) {
+      fa = lane_sum<LANES>(fa);
+#pragma unroll
+      for (int k = 0; k < P; ++k) {
+        g[k] = lane_sum<LANES>(g[k]);
+        hd[k] = lane_sum<LANES>(hd[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < H; ++k) h[k] = lane_sum<LANES>(h[k]);
     }
     f = fa;
     fend = f;
@@ -517,14 +547,17 @@ PCGB_HD void lm_iterate(const CF& cf, const TA (&d)[M], TA (&p)[Model::P], const
 #pragma unroll
     for (int k = 0; k < P; ++k) pt[k] = p[k] - stp[k];
     TA ftp = TA(0);
-#pragma unroll (sample_unroll<TA, TS, M>())
-    for (int i = 0; i < M; ++i) {
+#pragma unroll (sample_unroll<TA, TS, ML>())
+    for (int i = 0; i < ML; ++i) {
+      const int smp = i * LANES + sub;
+      if (LANES > 1 && smp >= M) break;
       TA c[C > 0 ? C : 1];
 #pragma unroll
-      for (int k = 0; k < C; ++k) c[k] = cf(k, i);
+      for (int k = 0; k < C; ++k) c[k] = cf(k, smp);
       const TA r = Model::template value<TA>(pt, c) - d[i];
       ftp += r * r;
     }
+    if constexpr (LANES > 1) ftp = lane_sum<LANES>(ftp);
 
     // gain ratio in TS (lsqnonlin.py:441-491)
     bool accept, very_good, pred_neg;
@@ -645,15 +678,19 @@ struct NoEpilogue {
 // and the samples still in registers and the cost at the final parameters
 // where the iterations evaluated it (NaN otherwise; see lm_iterate). A voxel
 // converged before the call loads p and d for the epilogue.
-template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B, class Epi = NoEpilogue>
-PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = Epi{}) {
-  constexpr int P = Model::P, H = Model::H, C = Model::C;
+// With LANES > 1 the voxel's samples are split over LANES adjacent lanes
+// (lane `sub` of them; see lm_iterate) and lane 0 writes the results.
+template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B, int LANES = 1,
+          class Epi = NoEpilogue>
+PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = Epi{}, int sub = 0) {
+  static_assert(LANES == 1 || !Epi::kActive, "epilogues run with one lane per voxel");
+  constexpr int P = Model::P, H = Model::H, C = Model::C, ML = lane_samples<M, LANES>();
   const long long N = a.N;
   const bool fresh = (a.flags & PCGB_LM_FRESH) != 0;
   if (!fresh && a.step_type[v] == 0) {
     // converged before this call (lsqnonlin.py:1000-1002): nothing changes,
     // first_f / last_f are copies of f as in the reference's host loop
-    if (a.iters > 0) {
+    if (a.iters > 0 && sub == 0) {
       const TA f0 = load<TA>(a.f, v);
       static_cast<TA*>(a.first_f)[v] = f0;
       static_cast<TA*>(a.last_f)[v] = f0;
@@ -676,9 +713,12 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
     hi[k] = SHARED_B ? Num<TA>::sub(a, k) : load<TA>(a.ub, k * a.bstride + v);
     stp[k] = !fresh && a.step ? load<TA>(a.step, k * N + v) : TA(0);
   }
-  TA d[M];
+  TA d[ML];
 #pragma unroll
-  for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
+  for (int i = 0; i < ML; ++i) {
+    const int smp = i * LANES + sub;
+    d[i] = LANES == 1 || smp < M ? load<TA>(a.data, smp * N + v) : TA(0);
+  }
   TA cv[SHARED_C ? 1 : (C > 0 ? C * M : 1)];
   if (!SHARED_C) {
 #pragma unroll
@@ -694,12 +734,13 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = E
   TA fend;
 
   if constexpr (SHARED_C) {
-    lm_iterate<Model, M, TA, TS>(SharedConsts<TA, M>{a}, d, p, lo, hi, stp, lam, st, f, first, done, a.iters, tol, mu,
-                                 eta, acc, dec, fend);
+    lm_iterate<Model, M, TA, TS, LANES>(SharedConsts<TA, M>{a}, d, p, lo, hi, stp, lam, st, f, first, done, a.iters,
+                                        tol, mu, eta, acc, dec, fend, sub);
   } else {
-    lm_iterate<Model, M, TA, TS>(RegConsts<TA, M, (C > 0 ? C * M : 1)>{cv}, d, p, lo, hi, stp, lam, st, f, first,
-                                 done, a.iters, tol, mu, eta, acc, dec, fend);
+    lm_iterate<Model, M, TA, TS, LANES>(RegConsts<TA, M, (C > 0 ? C * M : 1)>{cv}, d, p, lo, hi, stp, lam, st, f,
+                                        first, done, a.iters, tol, mu, eta, acc, dec, fend, sub);
   }
+  if (LANES > 1 && sub != 0) return;
 
   TA* pars = static_cast<TA*>(a.pars);
 #pragma unroll

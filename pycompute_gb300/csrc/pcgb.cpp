@@ -488,7 +488,7 @@ int kernel_of(pcgb_fitter* ft, int slot, cudaKernel_t* out) {
 static_assert(sizeof(PcgbMultiParams) <= 32000, "multi-model launch parameters exceed the 32 KB kernel parameter limit");
 
 std::string multi_source(int n, const char* const* srcs, const char* const* structs, const int* P, const int* C,
-                         const int* M, int dtype, int sdtype, int block) {
+                         const int* M, int dtype, int sdtype, int block, const int* lanes) {
   const char* ta = dtype == PCGB_DTYPE_F64 ? "double" : "float";
   const char* ts = sdtype == PCGB_DTYPE_F64 ? "double" : "float";
   std::ostringstream s;
@@ -507,10 +507,14 @@ std::string multi_source(int n, const char* const* srcs, const char* const* stru
   }
   s << "struct PcgbDispatch {\n  static __device__ __forceinline__ void run(int k, const PcgbLmParams& a, long long base,"
        " int chunk, int lane) {\n    switch (k) {\n";
-  for (int k = 0; k < n; ++k)
-    s << "      case " << k << ":\n        for (int j = lane; j < chunk; j += 32) {\n"
+  // a model fitted with L lanes per voxel: lanes 2j, 2j + 1 (L = 2) share voxel j of each 16
+  for (int k = 0; k < n; ++k) {
+    const int L = lanes ? lanes[k] : 1;
+    s << "      case " << k << ":\n        for (int j = lane / " << L << "; j < chunk; j += " << 32 / L << ") {\n"
       << "          const long long v = base + j;\n          if (v < a.N) pcgb::lm_fit_voxel<" << structs[k] << ", "
-      << M[k] << ", " << ta << ", " << ts << ", true, true>(a, v);\n        }\n        break;\n";
+      << M[k] << ", " << ta << ", " << ts << ", true, true, " << L << ">(a, v, pcgb::NoEpilogue{}, lane % " << L
+      << ");\n        }\n        break;\n";
+  }
   s << "      default: break;\n    }\n  }\n};\n";
   s << "extern \"C\" __global__ void __launch_bounds__(" << block
     << ") pcgb_multi_lm(const PcgbMultiParams q) { pcgb::multi_grid<PcgbDispatch>(q); }\n";
@@ -596,7 +600,7 @@ int pcgb_fitter_create(const char* model_source, const char* model_struct, int n
 
 int pcgb_multi_create(int n_models, const char* const* model_sources, const char* const* model_structs,
                       const int* nparam, const int* nconst, const int* ndata, int dtype, int solve_dtype, int maxrreg,
-                      int block, const char* cache_dir, pcgb_multi** out) {
+                      int block, const int* lanes, const char* cache_dir, pcgb_multi** out) {
   g_err.clear();
   if (!out) return fail(PCGB_EINVAL, "out is NULL");
   *out = nullptr;
@@ -604,11 +608,13 @@ int pcgb_multi_create(int n_models, const char* const* model_sources, const char
   if (!model_sources || !model_structs || !nparam || !nconst || !ndata) return fail(PCGB_EINVAL, "model arrays missing");
   if (block < 32 || block > 1024 || block % 32) return fail(PCGB_EINVAL, "block must be a multiple of 32 up to 1024");
   if (maxrreg != 0 && (maxrreg < 32 || maxrreg > 255)) return fail(PCGB_EINVAL, "maxrreg must be 0 or 32..255");
-  for (int k = 0; k < n_models; ++k)
+  for (int k = 0; k < n_models; ++k) {
     if (int rc = validate_create(model_sources[k], model_structs[k], nparam[k], nconst[k], ndata[k], dtype, solve_dtype))
       return rc;
+    if (lanes && lanes[k] != 1 && lanes[k] != 2) return fail(PCGB_EINVAL, "lanes per voxel must be 1 or 2");
+  }
   const std::string src =
-      multi_source(n_models, model_sources, model_structs, nparam, nconst, ndata, dtype, solve_dtype, block);
+      multi_source(n_models, model_sources, model_structs, nparam, nconst, ndata, dtype, solve_dtype, block, lanes);
   std::vector<std::string> extra;
   if (maxrreg) extra.push_back("--maxrregcount=" + std::to_string(maxrreg));
   std::vector<char> cubin;

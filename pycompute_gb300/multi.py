@@ -6,12 +6,12 @@ kernel, whose warps claim chunks of voxels from a device work counter (a warp
 always runs a single model). ``capture(jobs, iters)`` records the work-counter
 reset and the launch in a CUDA graph for repeated fits of the same buffers.
 
-``autotune(...)`` picks threads per block, a register cap and the chunk size by
-timing short fits of a sample of every job, and caches the choice per GPU and
-model set in ``_build/autotune.json``. One voxel per thread is fixed: the LM
-state is P-dimensional and its solve is serial, so splitting a voxel's
-samples across lanes would add P + P(P+1)/2 + 1 warp reductions to every
-iteration.
+``autotune(...)`` picks threads per block, a register cap, the chunk size,
+the queue order and, per model, the warp lanes that share one voxel (1, or 2
+that split the voxel's samples and sum their shares of f, J^T r and the
+Hessian with 2 + P + P(P+1)/2 lane shuffles per iteration; the solve then runs
+on both lanes) by timing short fits of a sample of every job, and caches the
+choice per GPU and model set in ``_build/autotune.json``.
 """
 from __future__ import annotations
 
@@ -75,7 +75,8 @@ class MultiModelFitter:
 
     _programs: dict = {}
 
-    def __init__(self, models: list, dtype=torch.float32, solve_dtype=None, block: int = 128, maxrreg: int = 0):
+    def __init__(self, models: list, dtype=torch.float32, solve_dtype=None, block: int = 128, maxrreg: int = 0,
+                 lanes=None):
         self.dtype = _dtype(dtype)
         self.solve_dtype = _dtype(solve_dtype) if solve_dtype is not None else torch.float64
         self.models = []
@@ -83,6 +84,10 @@ class MultiModelFitter:
             gm = codegen.generate(m.expr, m.pars_str, m.consts_str)
             self.models.append((gm, int(ndata)))
         self.block, self.maxrreg = int(block), int(maxrreg)
+        # warp lanes per voxel, per model (1 or 2: two lanes split a voxel's samples)
+        self.lanes = [1] * len(self.models) if lanes is None else [int(x) for x in lanes]
+        if len(self.lanes) != len(self.models):
+            raise ValueError("one lanes-per-voxel entry per model")
         self._prog = None
         self._counter = None
         self.chunk = 64
@@ -98,7 +103,7 @@ class MultiModelFitter:
 
     def build(self):
         dev = torch.cuda.current_device()
-        key = (self.key(), self.block, self.maxrreg, dev)
+        key = (self.key(), self.block, self.maxrreg, tuple(self.lanes), dev)
         prog = MultiModelFitter._programs.get(key)
         if prog is None:
             n = len(self.models)
@@ -109,7 +114,7 @@ class MultiModelFitter:
             rc = _lib.lib().pcgb_multi_create(n, srcs, structs, ints([gm.P for gm, _ in self.models]),
                                               ints([gm.C for gm, _ in self.models]),
                                               ints([nd for _, nd in self.models]), _TD[self.dtype],
-                                              _TD[self.solve_dtype], self.maxrreg, self.block,
+                                              _TD[self.solve_dtype], self.maxrreg, self.block, ints(self.lanes),
                                               _lib.cache_dir().encode(), ctypes.byref(h))
             _lib.check("pcgb_multi_create", rc)
             prog = h
@@ -161,16 +166,18 @@ def _cache_path() -> str:
 
 def autotune(models: list, make_jobs, iters: int, dtype=torch.float32, solve_dtype=None,
              blocks=(64, 128, 256), maxrregs=(0, 128, 96), chunks=(32, 64, 128, 256), reps: int = 2,
-             use_cache: bool = True) -> dict:
-    """Pick (block, maxrreg, chunk) for a model set.
+             use_cache: bool = True, lane_options=(1, 2)) -> dict:
+    """Pick (block, maxrreg, chunk, order, lanes) for a model set.
 
     make_jobs() returns fresh MultiJob lists of a representative sample; each
     configuration is timed on it with CUDA events after one warm-up fit. The
-    result is cached per GPU name and model set.
+    launch shape is searched with one lane per voxel; then, model by model,
+    each other lanes-per-voxel option is tried on the best shape and kept if
+    the whole fit gets faster. The result is cached per GPU name and model set.
     """
     probe = MultiModelFitter(models, dtype, solve_dtype)
     gpu = torch.cuda.get_device_name()
-    key = f"{gpu}|{probe.key()}|{iters}"
+    key = f"{gpu}|{probe.key()}|{iters}|lanes{','.join(str(x) for x in lane_options)}"
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -206,8 +213,40 @@ def autotune(models: list, make_jobs, iters: int, dtype=torch.float32, solve_dty
                             times.append(s.elapsed_time(e))
                     results.append({"block": block, "maxrreg": maxrreg, "chunk": chunk, "order": order,
                                     "ms": min(times)})
-    best = min(results, key=lambda r: r["ms"])
-    out = dict(best, gpu=gpu, trials=results, tune_s=round(time.perf_counter() - t0, 2))
+    best = dict(min(results, key=lambda r: r["ms"]), lanes=[1] * len(models))
+
+    def time_lanes(lanes):
+        fitter = MultiModelFitter(models, dtype, solve_dtype, block=best["block"], maxrreg=best["maxrreg"],
+                                  lanes=lanes)
+        try:
+            fitter.build()
+        except _lib.PcgbError:
+            return None
+        times = []
+        for r in range(reps + 1):
+            for j, i0 in zip(jobs, inits):
+                j.reset(i0)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record()
+            fitter.fit(jobs, iters, chunk=best["chunk"], order=best["order"])
+            e.record()
+            torch.cuda.synchronize()
+            if r:
+                times.append(s.elapsed_time(e))
+        return min(times)
+
+    lane_trials = []
+    for k in range(len(models)):
+        for opt in lane_options:
+            if opt == best["lanes"][k]:
+                continue
+            lanes = list(best["lanes"])
+            lanes[k] = opt
+            ms = time_lanes(lanes)
+            lane_trials.append({"lanes": lanes, "ms": ms})
+            if ms is not None and ms < best["ms"]:
+                best.update(lanes=lanes, ms=ms)
+    out = dict(best, gpu=gpu, trials=results, lane_trials=lane_trials, tune_s=round(time.perf_counter() - t0, 2))
     cache[key] = out
     os.makedirs(os.path.dirname(path), exist_ok=True)
     with open(path, "w") as f:

@@ -6,9 +6,9 @@ Warm-started fit (``WarmStartFitter.fit``):
   2. the LM runs ``iters_warm`` iterations from there, starting with a small
      damping ``lam0`` (the start is already close: the reference's lam = 5
      would shrink the first steps to a sixth of a Gauss-Newton step);
-  3. a voxel is flagged when its warm fit lands on a bound, has a non-finite
-     cost, or does not end below the cost of the constant initialisation
-     (the plain fitter's starting point);
+  3. in the same kernel, a voxel is flagged when its warm fit lands on a
+     bound, has a non-finite cost, or does not end below the cost of the
+     constant initialisation (the plain fitter's starting point);
   4. flagged voxels are compacted into an index list and refitted by the
      plain LM from the constant initialisation for ``iters_fallback``
      iterations in one launch over that list;
@@ -269,16 +269,16 @@ class WarmStartFitter:
         return self._buf
 
     def fit(self, data: torch.Tensor, iters_warm: int, iters_fallback: int, pars_out: torch.Tensor | None = None,
-            lam0: float = 1e-3, timings: dict | None = None, fused="select", events: list | None = None):
+            lam0: float = 1e-3, timings: dict | None = None, fused="lean", events: list | None = None):
         """Warm-started fit of data (M, N); returns a WarmFit.
 
-        ``fused="select"`` (default) runs the fallback check as its own kernel
-        and the select as the epilogue of the refit launch;
-        ``fused="lean"`` runs the warm LM and the check as one kernel (the
-        warm fit's cost taken from the iterations instead of re-evaluated; the
-        same rule, its cost comparisons on costs rounded differently, so a
-        voxel whose two costs tie to rounding may be flagged differently) and
-        the select as the refit's epilogue;
+        ``fused="lean"`` (default) runs the warm LM from a fresh start and
+        the check as one kernel (the warm fit's cost taken from the iterations
+        instead of re-evaluated; the same rule, its cost comparisons on costs
+        rounded differently, so a voxel whose two costs tie to rounding may be
+        flagged differently) and the select as the refit's epilogue;
+        ``fused="select"`` runs the fallback check as its own kernel and the
+        select as the epilogue of the refit launch;
         ``fused="epilogue"`` also runs the check as the epilogue of the warm
         LM launch (the signals are read once, but the LM kernel then holds
         more registers); ``fused=True`` runs check, refit and select as three

@@ -67,6 +67,8 @@ class WarmStartMLP:
             raise ValueError("nout must be 1..8")
         self.nin, self.nout = nin, nout
         self.log_in = bool(log_in)
+        # training GEMMs: "tcgen05" (tensor memory accumulators) or "mma" (warp-level mma.sync)
+        self.gemm_impl = "tcgen05"
         self.kinds = list(kinds)
         self.lb = [float(x) for x in lb]
         self.ub = [float(x) for x in ub]
@@ -162,10 +164,23 @@ class WarmStartMLP:
 
     def _gemm(self, a_layout, b_layout, epi, A, lda, Bm, ldb, M, N, K, k_split=0, bias=None, bias_stride=0,
               out_f32=None, ldo=0, out_bf16=None, ldob=0, zin=None, ldz=0):
+        if self.gemm_impl == "tcgen05":
+            if getattr(self, "_gemm_status", None) is None:
+                self._gemm_status = torch.zeros(1, dtype=torch.int32, device=self.device)
+            rc = _lib.lib().pcgb_gemm_bf16_tc(a_layout, b_layout, epi, _p(A), lda, _p(Bm), ldb, M, N, K, k_split,
+                                              bias, bias_stride, _p(out_f32), ldo, _p(out_bf16), ldob, _p(zin),
+                                              ldz, _p(self._gemm_status), _stream())
+            _lib.check("pcgb_gemm_bf16_tc", rc)
+            return
         rc = _lib.lib().pcgb_gemm_bf16(a_layout, b_layout, epi, _p(A), lda, _p(Bm), ldb, M, N, K, k_split,
                                        bias, bias_stride, _p(out_f32), ldo, _p(out_bf16), ldob, _p(zin), ldz,
                                        _stream())
         _lib.check("pcgb_gemm_bf16", rc)
+
+    def gemm_status(self) -> int:
+        """Nonzero if a tcgen05 training GEMM gave up on a bounded wait (reads the device flag)."""
+        st = getattr(self, "_gemm_status", None)
+        return 0 if st is None else int(st.item())
 
     def _bias_ptr(self, L: _Layer):
         return ctypes.c_void_p(L.master.data_ptr() + 4 * L.fan_in)

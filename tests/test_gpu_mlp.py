@@ -20,9 +20,10 @@ pytestmark = pytest.mark.gpu
 DEV = "cuda:0"
 
 
+@pytest.mark.parametrize("impl", ["tcgen05", "mma"])
 @pytest.mark.parametrize("a_layout,b_layout", [(0, 0), (0, 1), (1, 0), (1, 1)])
-@pytest.mark.parametrize("M,N,K", [(64, 64, 32), (200, 136, 128), (8, 136, 4096), (4096, 8, 16)])
-def test_gemm_layouts(a_layout, b_layout, M, N, K):
+@pytest.mark.parametrize("M,N,K", [(64, 64, 32), (200, 136, 128), (8, 136, 4096), (4096, 8, 16), (136, 24, 8)])
+def test_gemm_layouts(a_layout, b_layout, M, N, K, impl):
     rng = np.random.default_rng(M + N + K)
     A = mo.bf16(rng.standard_normal((M, K)))
     Bm = mo.bf16(rng.standard_normal((K, N)))
@@ -32,6 +33,7 @@ def test_gemm_layouts(a_layout, b_layout, M, N, K):
     ta = torch.from_numpy(np.ascontiguousarray(At)).to(DEV, torch.bfloat16)
     tb = torch.from_numpy(np.ascontiguousarray(Bt)).to(DEV, torch.bfloat16)
     net = WarmStartMLP(16, 4, [0, 1, 2, 2], [0] * 4, [1] * 4, DEV)
+    net.gemm_impl = impl
     for epi, ksplit in ((4, 0), (3, 256)):
         out = torch.zeros((M, N), device=DEV)
         net._gemm(a_layout, b_layout, epi, ta, ta.shape[1], tb, tb.shape[1], M, N, K, k_split=ksplit,
@@ -39,6 +41,43 @@ def test_gemm_layouts(a_layout, b_layout, M, N, K):
         torch.cuda.synchronize()
         got = out.cpu().numpy()
         assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max() + 1e-6
+    assert net.gemm_status() == 0
+
+
+@pytest.mark.parametrize("a_layout,b_layout", [(0, 0), (0, 1), (1, 1)])
+@pytest.mark.parametrize("epi", [0, 1, 2])
+def test_tcgen05_gemm_epilogues_match_mma(a_layout, b_layout, epi):
+    """The fused epilogues of the training step (bias + GELU with the
+    pre-activation and bf16 activation stored, bias only, GELU' times the
+    gradient) on the tcgen05 GEMM equal the mma.sync GEMM's up to fp32
+    summation order: fp32 outputs to 1e-5 of the largest, bf16 outputs
+    within one bf16 ulp."""
+    M, N, K = 1000, 136, 128
+    rng = np.random.default_rng(epi * 7 + a_layout)
+    A = mo.bf16(rng.standard_normal((M, K)) * 0.3)
+    Bm = mo.bf16(rng.standard_normal((K, N)) * 0.3)
+    At = A if a_layout == 0 else A.T
+    Bt = Bm.T if b_layout == 0 else Bm
+    ta = torch.from_numpy(np.ascontiguousarray(At)).to(DEV, torch.bfloat16)
+    tb = torch.from_numpy(np.ascontiguousarray(Bt)).to(DEV, torch.bfloat16)
+    bias = torch.from_numpy(rng.standard_normal(N).astype(np.float32)).to(DEV)
+    zin = torch.from_numpy(rng.standard_normal((M, N)).astype(np.float32)).to(DEV)
+    outs = []
+    for impl in ("mma", "tcgen05"):
+        net = WarmStartMLP(16, 4, [0, 1, 2, 2], [0] * 4, [1] * 4, DEV)
+        net.gemm_impl = impl
+        of = torch.zeros((M, N), device=DEV)
+        ob = torch.zeros((M, N), dtype=torch.bfloat16, device=DEV)
+        net._gemm(a_layout, b_layout, epi, ta, ta.shape[1], tb, tb.shape[1], M, N, K,
+                  bias=ctypes.c_void_p(bias.data_ptr()), bias_stride=1, out_f32=of, ldo=N, out_bf16=ob, ldob=N,
+                  zin=zin, ldz=N)
+        torch.cuda.synchronize()
+        assert net.gemm_status() == 0
+        outs.append((of.cpu().numpy(), ob.float().cpu().numpy()))
+    (f0, b0), (f1, b1) = outs
+    assert np.abs(f1 - f0).max() <= 1e-5 * max(np.abs(f0).max(), 1e-30)
+    ulp = np.maximum(np.abs(b0), 1e-30) * 2.0 ** -7
+    assert np.all(np.abs(b1 - b0) <= ulp + 1e-6)
 
 
 def _ivim16_batch(B, seed=0):

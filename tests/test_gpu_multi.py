@@ -73,3 +73,30 @@ def test_autotune_picks_and_caches():
     again = autotune(models, lambda: _jobs(ws, gens), iters=10, blocks=(64, 128), maxrregs=(0, 128),
                      chunks=(32, 128))
     assert again["block"] == best["block"] and again["chunk"] == best["chunk"]
+
+
+def test_two_lanes_per_voxel_match_one_lane():
+    """Two lanes per voxel (each accumulates half of the samples; the shares
+    are summed across the pair) against one lane per voxel, in one launch of
+    the four models: after one iteration every parameter agrees to fp32
+    summation order (1e-5 on all but a handful of entries); after 60 iterations
+    the fits agree to the fp32 noise floor of two summation orders."""
+    ws, gens = _make(4000, seed=11)
+    models = [(Expr(w.expr, w.pars, w.consts), w.M) for w in ws]
+    res = {}
+    for lanes in ([1, 1, 1, 1], [2, 2, 2, 2]):
+        fitter = MultiModelFitter(models, lanes=lanes)
+        for iters in (1, 60):
+            jobs = _jobs(ws, gens)
+            fitter.fit(jobs, iters)
+            torch.cuda.synchronize()
+            res[(lanes[0], iters)] = [(j.pars.cpu().numpy(), j.step_type.cpu().numpy(), j.iters.cpu().numpy())
+                                      for j in jobs]
+    for w, a, b in zip(ws, res[(1, 1)], res[(2, 1)]):
+        rel = parity.rel_err(b[0], a[0])
+        assert float((rel <= 1e-5).mean()) > 0.999, (w.name, float((rel <= 1e-5).mean()))
+        assert float((b[1] == a[1]).mean()) > 0.999, w.name
+    for w, a, b in zip(ws, res[(1, 60)], res[(2, 60)]):
+        rep = parity.compare_params(b[0], a[0])
+        assert rep["median_rel"] <= 1e-5 and rep["frac_gt_1e-4"] <= 0.12, (w.name, rep)
+        assert (b[2] > 0).all()

@@ -161,13 +161,16 @@ def test_lean_warm_lm_with_check_epilogue_matches_select_pipeline(per_voxel_boun
     np.testing.assert_allclose(c1[both], c0[both], rtol=1e-5)
 
 
-def test_fallback_flags_match_the_rule_on_the_oracle():
+@pytest.mark.parametrize("kernel", ["check", "lean"])
+def test_fallback_flags_match_the_rule_on_the_oracle(kernel):
     """The fused check's flagged set against the fallback rule evaluated on the
     CPU by the oracle, on the same warm fits: a voxel is flagged when its cost
     is not finite or not below the cost at the plain fitter's constant start,
     or a parameter is not strictly inside its bounds. GPU and oracle costs
     differ by fp32 rounding, so the two sets may differ only on voxels whose
-    two costs are within 1e-5 relative of each other."""
+    two costs are within 1e-5 relative of each other. ``check``: the check as
+    its own kernel after the warm LM; ``lean``: the check as the epilogue of
+    the warm LM from a fresh start (the warm cost taken from the iterations)."""
     from oracle import OracleModel
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     _, data = pipeline.synth_gpu(w, 50001, seed=9, device=DEV)
@@ -176,12 +179,20 @@ def test_fallback_flags_match_the_rule_on_the_oracle():
     pars = wf.net.infer(data)
     solm = wf._fitter()
     prot, lb, ub = wf._consts(DEV)
-    solm.setup(pars, prot, data, lb, ub)
-    solm.lam_t.fill_(3e-3)
-    solm.run(2)
-    warm = pars.cpu().numpy().copy()
     b = wf._buffers(w.P, N, DEV)
-    wf._warm_check(solm, data, pars, b)
+    if kernel == "check":
+        solm.setup(pars, prot, data, lb, ub)
+        solm.lam_t.fill_(3e-3)
+        solm.run(2)
+        warm = pars.cpu().numpy().copy()
+        wf._warm_check(solm, data, pars, b)
+    else:
+        warm_t = pars.clone()
+        solm.setup(warm_t, prot, data, lb, ub, init_state=False)
+        solm.run_fresh(2, 3e-3)
+        warm = warm_t.cpu().numpy().copy()
+        solm.setup(pars, prot, data, lb, ub, init_state=False)
+        wf._warm_lm_check(solm, data, pars, b, 2, 3e-3)
     torch.cuda.synchronize()
     n_fb = int(b["counts"][0].item())
     flagged_gpu = np.zeros(N, dtype=bool)
