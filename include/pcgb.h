@@ -194,8 +194,8 @@ int pcgb_warm_check(pcgb_fitter* fitter, const void* consts, int64_t consts_stri
  * cost is the one the iterations evaluated at the final parameters (NaN in
  * cost and cost_backup where they did not: the last accepted step was moved
  * by a bound, which flags the voxel; the select evaluates such a cost), so
- * only the cost at the constant start is computed. block: threads per block
- * (0 = default). nprobs < 2^31.
+ * only the cost at the constant start is computed (and, with iters = 0, the
+ * cost at params). block: threads per block (0 = default). nprobs < 2^31.
  */
 int pcgb_warm_lm_check(pcgb_fitter* fitter, const void* consts, int64_t consts_stride, const void* data,
                        const void* lower_bound, const void* upper_bound, int64_t bounds_stride, double tol, double mu,
@@ -517,10 +517,12 @@ int pcgb_mlp_prepare(const float* signals, int64_t n, int nin, int log_in, void*
 
 /* The network's activation elementwise, for checks against other
  * implementations: gelu_out[i] = gelu(z[i]) and grad_out[i] = gelu'(z[i]) as
- * every network kernel computes them (GELU in bf16x2 arithmetic with
- * tanh.approx.bf16x2; see the training and inference kernels). Either output
+ * every network kernel computes them for the units of network column
+ * `column` (>= 0): columns with column % 16 < 6 evaluate GELU by a polynomial
+ * in f16x2 arithmetic on the FMA pipe, the others in bf16x2 arithmetic with
+ * tanh.approx.bf16x2 (see the training and inference kernels). Either output
  * may be NULL. No reference counterpart. */
-int pcgb_mlp_gelu(const float* z, int64_t n, float* gelu_out, float* grad_out, void* stream);
+int pcgb_mlp_gelu(const float* z, int64_t n, int column, float* gelu_out, float* grad_out, void* stream);
 
 /* Fused inference of all four layers: signals (nin, n) -> initial parameters
  * out (nout, n), clamped to [lb, ub]; log_in selects the input transform the

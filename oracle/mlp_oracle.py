@@ -56,16 +56,74 @@ def _tanh_bf16(z):
         return zb, _trunc_bf16(np.tanh(u))
 
 
-def gelu(z):
+def _gelu_tanh(z):
     """GELU, tanh form (Hendrycks & Gimpel 2016), as the GPU kernels compute it
     in bf16x2 arithmetic: half of bf16(z t + z) (one fused rounding)."""
     zb, t = _tanh_bf16(z)
     return 0.5 * bf16_exact(zb * t + zb)
 
 
-def gelu_grad(z):
+def _gelu_tanh_grad(z):
     _, t = _tanh_bf16(z)
     return 0.5 * (1.0 + t) + 0.5 * z * (1.0 - t * t) * _C * (1.0 + 3 * 0.044715 * z * z)
+
+
+# The polynomial recipe of the columns n with n % 16 < POLY_COLS (the GPU's
+# FMA-pipe GELU): 2 gelu(z) ~ z + relu(|z| - 3) + E(min(z^2, 9)),
+# E(w) = w (q1 + w (q2 + w (q3 + w q4))), every operation in f16 with one
+# rounding (products of f16 values and their sums are exact in float64, so
+# rounding the float64 result once to f16 is the fused operation's rounding),
+# then the f16 result rounded to bf16.
+POLY_COLS = 6
+_Q = (0.7880859375, -0.11566162109375, 0.0112457275390625, -0.0004475116729736328)
+
+
+def _f16(x):
+    with np.errstate(over="ignore", invalid="ignore"):
+        return np.asarray(x, dtype=np.float64).astype(np.float16).astype(np.float64)
+
+
+def _gelu_poly(z):
+    zh = _f16(np.asarray(z, dtype=np.float32).astype(np.float64))
+    with np.errstate(over="ignore", invalid="ignore"):
+        w = np.fmin(_f16(zh * zh), 9.0)
+        e = _f16(_Q[3] * w + _Q[2])
+        e = _f16(e * w + _Q[1])
+        e = _f16(e * w + _Q[0])
+        e = _f16(e * w)
+        t = np.maximum(_f16(np.abs(zh) - 3.0), 0.0)
+        g = _f16(_f16(zh + t) + e)
+        return 0.5 * bf16_exact(g)
+
+
+def _gelu_poly_grad(z):
+    z = np.asarray(z, dtype=np.float64)
+    w = z * z
+    de = _Q[0] + 2 * _Q[1] * w + 3 * _Q[2] * w * w + 4 * _Q[3] * w ** 3
+    inner = 0.5 * (1.0 + 2.0 * z * de)
+    return np.where(np.abs(z) >= 3.0, np.where(z > 0, 1.0, 0.0), inner)
+
+
+def _by_column(fp, ft, z, col):
+    z = np.asarray(z)
+    if col is None:
+        cols = np.arange(z.shape[-1]) if z.ndim >= 1 else np.array(0)
+    else:
+        cols = np.asarray(col)
+    poly = (cols % 16) < POLY_COLS
+    return np.where(poly, fp(z), ft(z))
+
+
+def gelu(z, col=None):
+    """The network's activation of z; col: the network column of each entry
+    (default: the position along the last axis, as in a (batch x units)
+    array). Columns with col % 16 < POLY_COLS use the polynomial recipe, the
+    others the tanh recipe."""
+    return _by_column(_gelu_poly, _gelu_tanh, z, col)
+
+
+def gelu_grad(z, col=None):
+    return _by_column(_gelu_poly_grad, _gelu_tanh_grad, z, col)
 
 
 def split(Wfull, fan_in, rows_live):

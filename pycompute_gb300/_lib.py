@@ -112,7 +112,7 @@ SIGNATURES = {
                                ctypes.c_float, ctypes.c_float, ctypes.c_float, c_void_p, c_void_p]),
     "pcgb_mlp_prepare": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_i64, c_void_p, c_void_p, c_int, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_i64, c_void_p]),
-    "pcgb_mlp_gelu": (c_int, [c_void_p, c_i64, c_void_p, c_void_p, c_void_p]),
+    "pcgb_mlp_gelu": (c_int, [c_void_p, c_i64, c_int, c_void_p, c_void_p, c_void_p]),
     "pcgb_mlp_forward": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
     "pcgb_mlp_forward_tc": (c_int, [c_void_p, c_i64, c_int, c_int, c_void_p, c_void_p, c_int, c_void_p, c_void_p,

@@ -193,11 +193,12 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
         if (EPI == EPI_FWD_GELU) {
           const float z = acc + g.bias[n * g.bias_stride];
           g.out_f32[m * g.ldo + n] = z;
-          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(pcgb_mlp::gelu(z));
+          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(pcgb_mlp::gelu_col(z, int(n)));
         } else if (EPI == EPI_FWD_LINEAR) {
           g.out_f32[m * g.ldo + n] = acc + g.bias[n * g.bias_stride];
         } else if (EPI == EPI_BWD_DGELU) {
-          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(acc * pcgb_mlp::gelu_grad(g.zin[m * g.ldz + n]));
+          g.out_bf16[m * g.ldob + n] =
+              __float2bfloat16_rn(acc * pcgb_mlp::gelu_grad_col(g.zin[m * g.ldz + n], int(n)));
         } else if (EPI == EPI_DW_ATOMIC) {
           atomicAdd(&g.out_f32[m * g.ldo + n], acc);
         } else {

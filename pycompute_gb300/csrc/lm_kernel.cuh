@@ -1143,17 +1143,19 @@ __device__ void lm_check_grid(const PcgbLmParams& a) {
 }
 
 // The check of one voxel as the epilogue of its warm LM fit (lm_warm_grid):
-// the cost at the warm fit comes from the iterations (c, NaN where they did
+// the cost at the warm fit comes from the iterations (c; NaN where they did
 // not evaluate it: the last accepted step was moved by a bound, and the voxel
-// is flagged for being on the bound anyway), so only the cost at the constant
-// start is evaluated. Same rule, compaction, backup and state reset as
-// warm_check_voxel; the flagged voxels of each group of lanes that reaches
-// this point together are compacted with one atomic (any grouping gives a
-// valid list).
+// is flagged for being on the bound anyway - the select evaluates that cost -
+// or no iteration ran, and it is evaluated here), so in general only the
+// cost at the constant start is evaluated. Same rule, compaction, backup and
+// state reset as warm_check_voxel; the flagged voxels of each group of lanes
+// that reaches this point together are compacted with one atomic (any
+// grouping gives a valid list).
 template <class Model, int M, typename TA, bool SHARED_C>
 __device__ void warm_flag_voxel(const PcgbLmParams& a, long long v, const TA (&p)[Model::P], const TA (&d)[M], TA c) {
   constexpr int P = Model::P;
   const long long N = a.N;
+  if (a.iters == 0) c = voxel_cost<Model, M, TA, SHARED_C>(a, v, p, d);
   TA p0[P];
   TA mx = -Num<TA>::inf();
 #pragma unroll

@@ -169,11 +169,11 @@ __global__ void __launch_bounds__(128) gemm_bf16_kernel(const GemmArgs g) {
         if (EPI == EPI_FWD_GELU) {
           const float z = v + g.bias[n * g.bias_stride];
           g.out_f32[m * g.ldo + n] = z;
-          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(gelu(z));
+          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(gelu_col(z, int(n)));
         } else if (EPI == EPI_FWD_LINEAR) {
           g.out_f32[m * g.ldo + n] = v + g.bias[n * g.bias_stride];
         } else if (EPI == EPI_BWD_DGELU) {
-          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(v * gelu_grad(g.zin[m * g.ldz + n]));
+          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(v * gelu_grad_col(g.zin[m * g.ldz + n], int(n)));
         } else if (EPI == EPI_DW_ATOMIC) {
           atomicAdd(&g.out_f32[m * g.ldo + n], v);
         } else {
@@ -296,16 +296,17 @@ struct InferSmem {
 };
 
 // pre-activations (16 voxels x 128 in 16 n8 tiles, bias included) -> 2 GELU ->
-// bf16 A fragments of the next layer (8 k16 tiles), whose weights are staged halved
-__device__ __forceinline__ void act_to_afrag(const float (&acc)[16][4], uint32_t (&a)[8][4]) {
+// bf16 A fragments of the next layer (8 k16 tiles), whose weights are staged
+// halved; this lane's columns are 16 kt + 2 tq (+ 1) and 16 kt + 8 + 2 tq (+ 1)
+__device__ __forceinline__ void act_to_afrag(const float (&acc)[16][4], uint32_t (&a)[8][4], int tq) {
 #pragma unroll
   for (int kt = 0; kt < 8; ++kt) {
     const float* lo = acc[2 * kt];
     const float* hi = acc[2 * kt + 1];
-    a[kt][0] = gelu2x_pack_bf16(lo[0], lo[1]);
-    a[kt][1] = gelu2x_pack_bf16(lo[2], lo[3]);
-    a[kt][2] = gelu2x_pack_bf16(hi[0], hi[1]);
-    a[kt][3] = gelu2x_pack_bf16(hi[2], hi[3]);
+    a[kt][0] = gelu2x_col_pack_bf16(lo[0], lo[1], 2 * tq);
+    a[kt][1] = gelu2x_col_pack_bf16(lo[2], lo[3], 2 * tq);
+    a[kt][2] = gelu2x_col_pack_bf16(hi[0], hi[1], 8 + 2 * tq);
+    a[kt][3] = gelu2x_col_pack_bf16(hi[2], hi[3], 8 + 2 * tq);
   }
 }
 
@@ -408,11 +409,11 @@ __global__ void __launch_bounds__(384, 1) mlp_infer_kernel(const InferArgs p) {
       }
     }
     uint32_t af[8][4];
-    act_to_afrag(acc, af);
+    act_to_afrag(acc, af, lane & 3);
     hidden_layer<NIN>(S.w2, S.b2, af, acc, lane);
-    act_to_afrag(acc, af);
+    act_to_afrag(acc, af, lane & 3);
     hidden_layer<NIN>(S.w3, S.b3, af, acc, lane);
-    act_to_afrag(acc, af);
+    act_to_afrag(acc, af, lane & 3);
     float y[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int kt = 0; kt < 8; ++kt) {
@@ -454,12 +455,13 @@ cudaError_t launch_gemm(int epi, const GemmArgs& g, dim3 grid, cudaStream_t s) {
   return cudaGetLastError();
 }
 
-// elementwise gelu(z) and gelu'(z) of the network's activation recipe
-__global__ void gelu_eval_kernel(const float* z, long long n, float* g, float* dg) {
+// elementwise gelu(z) and gelu'(z) of the network's activation recipe for
+// the units of network column `col`
+__global__ void gelu_eval_kernel(const float* z, long long n, int col, float* g, float* dg) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  if (g) g[i] = gelu(z[i]);
-  if (dg) dg[i] = gelu_grad(z[i]);
+  if (g) g[i] = gelu_col(z[i], col);
+  if (dg) dg[i] = gelu_grad_col(z[i], col);
 }
 
 }  // namespace pcgb_mlp
@@ -468,12 +470,13 @@ using namespace pcgb_mlp;
 
 extern "C" {
 
-int pcgb_mlp_gelu(const float* z, int64_t n, float* gelu_out, float* grad_out, void* stream) {
-  if (n < 0 || (n > 0 && !z)) return mlp_fail(PCGB_EINVAL, "bad gelu arguments");
+int pcgb_mlp_gelu(const float* z, int64_t n, int column, float* gelu_out, float* grad_out, void* stream) {
+  if (n < 0 || (n > 0 && !z) || column < 0) return mlp_fail(PCGB_EINVAL, "bad gelu arguments");
   if (n == 0) return PCGB_OK;
   const long long blocks = (n + 255) / 256;
   if (blocks > 0x7fffffffLL) return mlp_fail(PCGB_ERANGE, "gelu: n too large");
-  gelu_eval_kernel<<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(z, n, gelu_out, grad_out);
+  gelu_eval_kernel<<<unsigned(blocks), 256, 0, static_cast<cudaStream_t>(stream)>>>(z, n, column, gelu_out,
+                                                                                       grad_out);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return mlp_fail(PCGB_ECUDA, cudaGetErrorString(e));
   return PCGB_OK;

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cstdint>
 
@@ -52,6 +53,61 @@ __device__ __forceinline__ float gelu_grad(float z) {
   const float t = __low2float(tanh_bf16x2(__float2bfloat162_rn(z)));
   return fmaf(0.5f, t, 0.5f) + 0.5f * z * (1.0f - t * t) * fmaf(0.1070322244089003f, z2, 0.7978845608028654f);
 }
+// GELU on the FMA pipe for a share of the columns. The tanh of the recipe
+// above takes the MUFU pipe (two MUFU operations per pair of activations,
+// 16 per SM per clock); the network's columns n with n % 16 < kPolyCols
+// instead evaluate the same GELU with no MUFU operation, by a polynomial in
+// f16x2 arithmetic:
+//   2 gelu(z) ~ z + relu(|z| - a) + E(min(z^2, a^2)),  a = 3,
+//   E(w) = w (q1 + w (q2 + w (q3 + w q4)))  ~  z tanh(u(z)) on |z| <= a,
+// with z rounded to f16 and every product and fused multiply-add rounded to
+// f16, then the f16 result rounded to bf16. q1..q4 are a near-minimax fit of
+// z tanh(u(z)) in w = z^2 on [0, 9], weighted by 1/|z| (Lawson's iteratively
+// reweighted least squares, C. L. Lawson 1961), rounded to f16 and adjusted
+// by single f16 ulps to minimise the maximum error of the whole recipe; its
+// error is at most 0.0126 |z| (the MUFU recipe's at most 0.0176 |z|) for
+// |z| < 32752 (beyond, the f16 sum overflows). The columns are fixed, so
+// training and inference see the same activation per unit.
+constexpr int kPolyCols = 6;
+__device__ __forceinline__ bool poly_col(int n) { return (n & 15) < kPolyCols; }
+__device__ __forceinline__ __half2 h2bits(uint32_t v) { return *reinterpret_cast<__half2*>(&v); }
+__device__ __forceinline__ uint32_t gelu2x_poly_pack_bf16(float z0, float z1) {
+  const __half2 q1 = h2bits(0x3a4e3a4eu), q2 = h2bits(0xaf67af67u), q3 = h2bits(0x21c221c2u),
+                q4 = h2bits(0x8f558f55u);
+  const __half2 a2 = h2bits(0x48804880u), one = h2bits(0x3c003c00u), neg_a = h2bits(0xc200c200u);
+  const __half2 zh = __floats2half2_rn(z0, z1);
+  const __half2 w = __hmin2(__hmul2(zh, zh), a2);
+  __half2 e = __hfma2(q4, w, q3);
+  e = __hfma2(e, w, q2);
+  e = __hfma2(e, w, q1);
+  e = __hmul2(e, w);
+  const __half2 t = __hfma2_relu(__habs2(zh), one, neg_a);
+  const float2 g = __half22float2(__hadd2(__hadd2(zh, t), e));
+  return pack_bf16(g.x, g.y);
+}
+// d gelu / dz of the polynomial recipe (fp32, exact derivative of the
+// continuous form)
+__device__ __forceinline__ float gelu_poly_grad(float z) {
+  const float q1 = 0.7880859375f, q2 = -0.11566162109375f, q3 = 0.0112457275390625f,
+              q4 = -0.0004475116729736328f;
+  const float az = fabsf(z);
+  if (az >= 3.0f) return z > 0.f ? 1.0f : 0.0f;  // 1/2 (1 + 1) or 1/2 (1 - 1)
+  const float w = z * z;
+  const float de = fmaf(fmaf(fmaf(4.f * q4, w, 3.f * q3), w, 2.f * q2), w, q1);  // E'(w)
+  return 0.5f * fmaf(2.f * z, de, 1.0f);
+}
+// column-aware activation: n = column of z0 (z1 is column n + 1, same choice
+// for even n)
+__device__ __forceinline__ uint32_t gelu2x_col_pack_bf16(float z0, float z1, int n) {
+  return poly_col(n) ? gelu2x_poly_pack_bf16(z0, z1) : gelu2x_pack_bf16(z0, z1);
+}
+__device__ __forceinline__ float gelu_col(float z, int n) {
+  return 0.5f * __low2float(bits_bf162(gelu2x_col_pack_bf16(z, z, n)));
+}
+__device__ __forceinline__ float gelu_grad_col(float z, int n) {
+  return poly_col(n) ? gelu_poly_grad(z) : gelu_grad(z);
+}
+
 // eight bf16 values times 1/2 (exact for normal numbers)
 __device__ __forceinline__ uint4 halve_bf16x8(uint4 v) {
   uint32_t* w = reinterpret_cast<uint32_t*>(&v);

@@ -104,7 +104,8 @@ __device__ void stage_weights(bf16* dst, const bf16* src, int rows, int rows_liv
   }
 }
 
-// 2 GELU of 16 pre-activations (columns [c0, c0 + 16), bias included), written
+// 2 GELU of 16 pre-activations (columns [c0, c0 + 16), bias included; c0 a
+// multiple of 16, so each column's recipe is fixed at compile time), written
 // as bf16 into row r of the next layer's A operand (row_base = its byte offset)
 __device__ __forceinline__ void gelu_row16(const uint32_t (&acc)[16], int c0, unsigned char* row_base) {
 #pragma unroll
@@ -114,7 +115,7 @@ __device__ __forceinline__ void gelu_row16(const uint32_t (&acc)[16], int c0, un
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       const int j = q * 8 + 2 * e;
-      w[e] = pcgb_mlp::gelu2x_pack_bf16(__uint_as_float(acc[j]), __uint_as_float(acc[j + 1]));
+      w[e] = pcgb_mlp::gelu2x_col_pack_bf16(__uint_as_float(acc[j]), __uint_as_float(acc[j + 1]), c0 + j);
     }
     *reinterpret_cast<uint4*>(row_base + ((c0 + q * 8) >> 3) * 128) = o;
   }

@@ -119,10 +119,11 @@ def test_run_rejects_null_fitter():
 
 def test_elementwise_gelu_rejects_bad_arguments_without_a_gpu():
     L = _lib.lib()
-    assert L.pcgb_mlp_gelu(None, 0, None, None, None) == 0
-    assert L.pcgb_mlp_gelu(None, 5, None, None, None) == -22
+    assert L.pcgb_mlp_gelu(None, 0, 0, None, None, None) == 0
+    assert L.pcgb_mlp_gelu(None, 5, 0, None, None, None) == -22
     assert L.pcgb_mlp_last_error()
-    assert L.pcgb_mlp_gelu(None, -1, None, None, None) == -22
+    assert L.pcgb_mlp_gelu(None, -1, 0, None, None, None) == -22
+    assert L.pcgb_mlp_gelu(None, 0, -1, None, None, None) == -22
 
 
 @pytest.mark.parametrize("entry", ["pcgb_multi_run", "pcgb_multi_run_noalloc"])

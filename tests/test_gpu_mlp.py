@@ -191,18 +191,18 @@ def test_gelu_recipe_matches_oracle():
     zt = torch.from_numpy(z).to(DEV)
     g = torch.empty_like(zt)
     dg = torch.empty_like(zt)
-    rc = _lib.lib().pcgb_mlp_gelu(ctypes.c_void_p(zt.data_ptr()), zt.numel(), ctypes.c_void_p(g.data_ptr()),
+    rc = _lib.lib().pcgb_mlp_gelu(ctypes.c_void_p(zt.data_ptr()), zt.numel(), 15, ctypes.c_void_p(g.data_ptr()),
                                   ctypes.c_void_p(dg.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     _lib.check("pcgb_mlp_gelu", rc)
     torch.cuda.synchronize()
     g, dg = g.cpu().numpy().astype(np.float64), dg.cpu().numpy().astype(np.float64)
-    want = mo.gelu(z)
+    want = mo.gelu(z, col=15)
     same = g == want
     assert same.mean() > 0.97, same.mean()
     zb = mo.bf16(z)
     assert np.all(np.abs(g - want) <= np.abs(zb) * 1.5 * 2.0 ** -8 + 1e-30), np.abs(g - want).max()
     zd = z.astype(np.float64)
-    want_d = mo.gelu_grad(zd)
+    want_d = mo.gelu_grad(zd, col=15)
     _, t = mo._tanh_bf16(z)
     k = np.sqrt(2 / np.pi) * (1 + 3 * 0.044715 * zd * zd)
     tol = (0.5 + np.abs(zd * t) * k) * np.maximum(np.abs(t), 2.0 ** -126) * 2.0 ** -7 + 1e-6 + 1e-5 * np.abs(want_d)
@@ -210,6 +210,31 @@ def test_gelu_recipe_matches_oracle():
     assert np.isclose(dg, want_d, rtol=1e-5, atol=1e-6).mean() > 0.95
     assert np.all(np.abs(dg - want_d) <= tol), np.max(np.abs(dg - want_d) / tol)
     assert g[np.where(z == 40.0)[0][0]] == 40.0 and g[np.where(z == -40.0)[0][0]] == 0.0
+
+
+def test_polynomial_gelu_matches_oracle_bit_for_bit():
+    """The FMA-pipe GELU of columns n % 16 < 6 (f16x2 polynomial, no MUFU
+    operation) equals the oracle's restatement of its f16 roundings bit for
+    bit, column 0 through 5 alike and columns 6 to 15 not; its fp32
+    derivative agrees with the oracle's float64 evaluation to 1e-5."""
+    rng = np.random.default_rng(6)
+    z = np.concatenate([np.linspace(-40, 40, 400001), rng.standard_normal(100000) * 3,
+                        [0.0, -0.0, 1e-30, -1e-30, 3.0, -3.0, 2.9999, -2.9999, 65000.0, -65000.0]]).astype(np.float32)
+    zt = torch.from_numpy(z).to(DEV)
+    for col in (0, 5, 16 * 7 + 2):
+        g = torch.empty_like(zt)
+        dg = torch.empty_like(zt)
+        rc = _lib.lib().pcgb_mlp_gelu(ctypes.c_void_p(zt.data_ptr()), zt.numel(), col, ctypes.c_void_p(g.data_ptr()),
+                                      ctypes.c_void_p(dg.data_ptr()),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        _lib.check("pcgb_mlp_gelu", rc)
+        torch.cuda.synchronize()
+        g, dg = g.cpu().numpy().astype(np.float64), dg.cpu().numpy().astype(np.float64)
+        fin = np.abs(z) < 32752
+        want = mo.gelu(z, col=col)
+        np.testing.assert_array_equal(g[fin], want[fin])
+        np.testing.assert_allclose(dg, mo.gelu_grad(z.astype(np.float64), col=col), rtol=1e-5, atol=1e-6)
+    assert not np.array_equal(mo.gelu(z, col=6), mo.gelu(z, col=0))
 
 
 def test_tcgen05_lost_wait_sets_status_frees_tmem_and_returns():

@@ -79,8 +79,12 @@ def test_two_lanes_per_voxel_match_one_lane():
     """Two lanes per voxel (each accumulates half of the samples; the shares
     are summed across the pair) against one lane per voxel, in one launch of
     the four models: after one iteration every parameter agrees to fp32
-    summation order (1e-5 on all but a handful of entries); after 60 iterations
-    the fits agree to the fp32 noise floor of two summation orders."""
+    summation order (1e-5 on all but a handful of entries); after 60
+    iterations both summation orders are equally close to the all-FP64 fit
+    (same LM, same start, same iterations): the two-lane median error at most
+    1.5 times the one-lane one (the ill-conditioned bi-exponential T2 fits
+    of the two orders differ from each other by more than either does from
+    the FP64 fit)."""
     ws, gens = _make(4000, seed=11)
     models = [(Expr(w.expr, w.pars, w.consts), w.M) for w in ws]
     res = {}
@@ -96,7 +100,14 @@ def test_two_lanes_per_voxel_match_one_lane():
         rel = parity.rel_err(b[0], a[0])
         assert float((rel <= 1e-5).mean()) > 0.999, (w.name, float((rel <= 1e-5).mean()))
         assert float((b[1] == a[1]).mean()) > 0.999, w.name
-    for w, a, b in zip(ws, res[(1, 60)], res[(2, 60)]):
-        rep = parity.compare_params(b[0], a[0])
-        assert rep["median_rel"] <= 1e-5 and rep["frac_gt_1e-4"] <= 0.12, (w.name, rep)
+    for w, (true, data, init, lb, ub, prot), a, b in zip(ws, gens, res[(1, 60)], res[(2, 60)]):
+        s64 = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float64)
+        p64 = torch.from_numpy(init.astype("float64")).to(DEV)
+        s64.setup(p64, list(w.protocol), torch.from_numpy(data).to(DEV).double(), list(w.lb), list(w.ub))
+        s64.run(60)
+        torch.cuda.synchronize()
+        ref = p64.cpu().numpy()
+        e1 = parity.compare_params(a[0], ref)["median_rel"]
+        e2 = parity.compare_params(b[0], ref)["median_rel"]
+        assert e2 <= 1.5 * e1 + 1e-7, (w.name, e1, e2)
         assert (b[2] > 0).all()

@@ -113,8 +113,8 @@ def test_fused_fallback_matches_separate_kernels(per_voxel_bounds, schedule, mod
     np.testing.assert_array_equal(c0, c1)
 
 
-@pytest.mark.parametrize("per_voxel_bounds", [False, True])
-def test_lean_warm_lm_with_check_epilogue_matches_select_pipeline(per_voxel_bounds):
+@pytest.mark.parametrize("per_voxel_bounds,iters", [(False, 3), (True, 3), (False, 0)])
+def test_lean_warm_lm_with_check_epilogue_matches_select_pipeline(per_voxel_bounds, iters):
     """The warm LM from a fresh start with the check as its epilogue
     (fused="lean") against the pipeline with the check as its own kernel
     (fused="select"): the same warm iterations and rule, but the warm fit's cost
@@ -122,7 +122,8 @@ def test_lean_warm_lm_with_check_epilogue_matches_select_pipeline(per_voxel_boun
     a decision compares differ by rounding. The flagged sets may differ only on
     voxels whose warm cost and constant-start cost tie to 1e-5; voxels flagged
     by neither end bit-equal; voxels flagged by both end equal unless the
-    select compared a tie (final costs within 1e-5)."""
+    select compared a tie (final costs within 1e-5). With no warm iteration
+    the epilogue evaluates the warm cost itself, as the check kernel does."""
     w = synth.ivim(synth.ivim_b16(), name="ivim16")
     _, data = pipeline.synth_gpu(w, 50001, seed=17, device=DEV)
     N = data.shape[1]
@@ -133,7 +134,7 @@ def test_lean_warm_lm_with_check_epilogue_matches_select_pipeline(per_voxel_boun
         wf = pipeline.WarmStartFitter(w, _BadNet(w))
         if per_voxel_bounds:
             wf._consts = lambda dev: (list(w.protocol), lbt, ubt)
-        res = wf.fit(data, iters_warm=3, iters_fallback=20, fused=fused)
+        res = wf.fit(data, iters_warm=iters, iters_fallback=20, fused=fused)
         torch.cuda.synchronize()
         flagged = np.zeros(N, dtype=bool)
         flagged[res.fallback_idx[:res.n_fallback].cpu().numpy()] = True
@@ -145,7 +146,7 @@ def test_lean_warm_lm_with_check_epilogue_matches_select_pipeline(per_voxel_boun
     warm = wf.net.infer(data)
     solm = wf._fitter()
     solm.setup(warm, list(w.protocol), data, list(w.lb), list(w.ub))
-    solm.run_fresh(3, 1e-3)
+    solm.run_fresh(iters, 1e-3)
     cw = solm.cost().cpu().numpy().astype(np.float64)
     cs = solm.cost(pipeline.init_constant(data, w.init_values)).cpu().numpy().astype(np.float64)
     torch.cuda.synchronize()

@@ -151,16 +151,43 @@ def test_bf16_rounding_helpers():
 
 
 def test_gelu_oracle_recipe():
-    """The oracle's GELU follows the bf16 recipe: exact 0 at 0, the identity
-    for large z, 0 for very negative z, and a leak of z 2^-9 where the
-    truncated tanh stops one ulp short of -1."""
+    """The oracle's GELU follows the bf16 tanh recipe on columns n % 16 >= 6:
+    exact 0 at 0, the identity for large z, 0 for very negative z, and a leak
+    of z 2^-9 where the truncated tanh stops one ulp short of -1."""
     from oracle import mlp_oracle as mo
     z = np.array([0.0, 10.0, -10.0, -4.0, 1.0])
-    g = mo.gelu(z)
+    g = mo.gelu(z, col=15)
     assert g[0] == 0.0 and g[1] == 10.0 and g[2] == 0.0
     assert g[3] == -4.0 * 2.0 ** -9
     exact = 0.5 * z * (1 + np.tanh(np.sqrt(2 / np.pi) * (z + 0.044715 * z ** 3)))
     assert abs(g[4] - exact[4]) < 4e-3
+
+
+def test_gelu_polynomial_recipe():
+    """The polynomial GELU of columns n % 16 < 6 (f16 arithmetic, no tanh):
+    exact 0 at 0, the identity beyond |z| = 3 for positive z and 0 for
+    negative z up to the polynomial's value at the clamp, within 0.0126 |z|
+    of the exact tanh-form GELU everywhere (the tanh recipe: 0.0176 |z|), and
+    its derivative is the derivative of the same function (checked against
+    central differences of the continuous form)."""
+    from oracle import mlp_oracle as mo
+    z = np.linspace(-12, 12, 480001).astype(np.float32).astype(np.float64)
+    g = mo.gelu(z, col=0)
+    exact = 0.5 * z * (1 + np.tanh(np.sqrt(2 / np.pi) * (z + 0.044715 * z ** 3)))
+    rel = np.abs(g - exact) / np.maximum(np.abs(z), 2.0 ** -6)
+    assert rel.max() <= 0.0126 / 2 + 1e-12, rel.max()
+    assert mo.gelu(np.array([0.0]), col=3)[0] == 0.0
+    assert np.all(mo.gelu(np.array([5.0, 7.5]), col=5) == np.array([5.0, 7.5]))
+    # the continuous form's derivative
+    q = mo._Q
+    zz = np.linspace(-2.99, 2.99, 2001)
+
+    def cont(x):
+        w = np.minimum(x * x, 9.0)
+        return 0.5 * (x + np.maximum(np.abs(x) - 3.0, 0.0) + w * (q[0] + w * (q[1] + w * (q[2] + w * q[3]))))
+    h = 1e-6
+    fd = (cont(zz + h) - cont(zz - h)) / (2 * h)
+    np.testing.assert_allclose(mo.gelu_grad(zz, col=1), fd, rtol=1e-6, atol=1e-8)
 
 
 @pytest.mark.skipif(not ref_available(10), reason="reference kernel not built (no reference tree)")
