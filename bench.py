@@ -1090,7 +1090,7 @@ def main():
         lm_gbs = bpv * N / (h["lm_ms"] / 1e3) / 1e9
         net_tf = NET_FLOP_PER_VOXEL * N / (h["net_ms"] / 1e3) / 1e12
         traffic = None
-        tf = os.path.join(ROOT, "profiles", "lm_ivim16_warm_traffic.json")
+        tf = os.path.join(ROOT, "profiles", "lmw_ivim16_warm_traffic.json")
         if os.path.exists(tf):
             with open(tf) as f:
                 traffic = json.load(f)["dram_bytes_per_voxel"] * N
@@ -1113,7 +1113,7 @@ def main():
                     "single_volume": {"value": ws * N / (h["e2e_single_ms"] / 1e3), "ms_per_step": h["e2e_single_ms"],
                                       "api": f"WarmStartFitter.fit_host, {h['e2e_chunks']} chunks"}},
             "roofline": {"bound": "hbm", "achieved": lm_gbs, "peak": hbm, "unit": "GB/s", "frac": lm_gbs / hbm,
-                         "traffic": traffic, "peak_source": peak_kind, "kernel": "pcgb_lm (warm LM stage)",
+                         "traffic": traffic, "peak_source": peak_kind, "kernel": "pcgb_lmw (warm LM with the fallback check as its epilogue)",
                          "algorithmic_bytes_per_voxel": bpv, "kernel_ms": h["lm_ms"],
                          "note": "per-voxel iterative solver: bound by the FP64 pipe (GMW81 solve + gain ratio), "
                                  "not by HBM; ncu summaries in profiles/"},
@@ -1127,16 +1127,17 @@ def main():
                                                  FP64_PER_SM_CLK, h["clocks"],
                                                  "FP64-pipe instructions (DFMA + DMUL + DADD) per voxel-iteration, "
                                                  "ncu opcode counts"),
-                                  kernel="pcgb_lm (warm LM stage)", bound="fp64 pipe"),
+                                  kernel="pcgb_lmw (warm LM with the fallback check as its epilogue)",
+                                  bound="fp64 pipe"),
             "warm_start": h["detail"],
             "plain_lm_ivim10_8.4M": ivim10,
             "mixed_batch": mixed,
             "precision_stress": stress,
             "cpu_baseline": cpu,
-            # our kernels per warm-start step: tcgen05 network, warm LM, fallback
-            # check, refit with select epilogue (counted from an ncu launch list of
-            # the timed steps; the state fills are PyTorch's)
-            "gpu_launches": 4 * args.steps,
+            # our kernels per warm-start step: tcgen05 network, warm LM with the
+            # fallback check as its epilogue, refit with the select as its
+            # epilogue (counted from an ncu launch list of the timed steps)
+            "gpu_launches": 3 * args.steps,
             "clocks": h["clocks"],
         }
         print(json.dumps(line), flush=True)

@@ -69,11 +69,11 @@ def _gelu_tanh_grad(z):
 
 
 # The polynomial recipe of the columns n with n % 16 < POLY_COLS (the GPU's
-# FMA-pipe GELU): 2 gelu(z) ~ z + relu(|z| - 3) + E(min(z^2, 9)),
-# E(w) = w (q1 + w (q2 + w (q3 + w q4))), every operation in f16 with one
-# rounding (products of f16 values and their sums are exact in float64, so
-# rounding the float64 result once to f16 is the fused operation's rounding),
-# then the f16 result rounded to bf16.
+# FMA-pipe GELU): 2 gelu(z) ~ (z + relu(|z| - 3)) + w e(w), w = min(z^2, 9),
+# e(w) = q1 + w (q2 + w (q3 + w q4)), the last step one fused multiply-add,
+# every operation in f16 with one rounding (products of f16 values and their
+# sums are exact in float64, so rounding the float64 result once to f16 is the
+# fused operation's rounding), then the f16 result rounded to bf16.
 POLY_COLS = 6
 _Q = (0.7880859375, -0.11566162109375, 0.0112457275390625, -0.0004475116729736328)
 
@@ -90,9 +90,8 @@ def _gelu_poly(z):
         e = _f16(_Q[3] * w + _Q[2])
         e = _f16(e * w + _Q[1])
         e = _f16(e * w + _Q[0])
-        e = _f16(e * w)
-        t = np.maximum(_f16(np.abs(zh) - 3.0), 0.0)
-        g = _f16(_f16(zh + t) + e)
+        s = _f16(zh + np.maximum(_f16(np.abs(zh) - 3.0), 0.0))
+        g = _f16(e * w + s)
         return 0.5 * bf16_exact(g)
 
 

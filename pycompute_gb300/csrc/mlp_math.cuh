@@ -58,10 +58,12 @@ __device__ __forceinline__ float gelu_grad(float z) {
 // 16 per SM per clock); the network's columns n with n % 16 < kPolyCols
 // instead evaluate the same GELU with no MUFU operation, by a polynomial in
 // f16x2 arithmetic:
-//   2 gelu(z) ~ z + relu(|z| - a) + E(min(z^2, a^2)),  a = 3,
-//   E(w) = w (q1 + w (q2 + w (q3 + w q4)))  ~  z tanh(u(z)) on |z| <= a,
-// with z rounded to f16 and every product and fused multiply-add rounded to
-// f16, then the f16 result rounded to bf16. q1..q4 are a near-minimax fit of
+//   2 gelu(z) ~ (z + relu(|z| - a)) + w e(w),  w = min(z^2, a^2),  a = 3,
+//   e(w) = q1 + w (q2 + w (q3 + w q4)),  w e(w) ~ z tanh(u(z)) on |z| <= a,
+// with z rounded to f16, every operation rounded once to f16 (the last one a
+// fused multiply-add; the product and sum use the non-contracting forms, so
+// the compiler cannot fuse them differently), then the f16 result rounded to
+// bf16. q1..q4 are a near-minimax fit of
 // z tanh(u(z)) in w = z^2 on [0, 9], weighted by 1/|z| (Lawson's iteratively
 // reweighted least squares, C. L. Lawson 1961), rounded to f16 and adjusted
 // by single f16 ulps to minimise the maximum error of the whole recipe; its
@@ -76,13 +78,12 @@ __device__ __forceinline__ uint32_t gelu2x_poly_pack_bf16(float z0, float z1) {
                 q4 = h2bits(0x8f558f55u);
   const __half2 a2 = h2bits(0x48804880u), one = h2bits(0x3c003c00u), neg_a = h2bits(0xc200c200u);
   const __half2 zh = __floats2half2_rn(z0, z1);
-  const __half2 w = __hmin2(__hmul2(zh, zh), a2);
+  const __half2 w = __hmin2(__hmul2_rn(zh, zh), a2);
   __half2 e = __hfma2(q4, w, q3);
   e = __hfma2(e, w, q2);
   e = __hfma2(e, w, q1);
-  e = __hmul2(e, w);
-  const __half2 t = __hfma2_relu(__habs2(zh), one, neg_a);
-  const float2 g = __half22float2(__hadd2(__hadd2(zh, t), e));
+  const __half2 s = __hadd2_rn(zh, __hfma2_relu(__habs2(zh), one, neg_a));
+  const float2 g = __half22float2(__hfma2(e, w, s));
   return pack_bf16(g.x, g.y);
 }
 // d gelu / dz of the polynomial recipe (fp32, exact derivative of the
