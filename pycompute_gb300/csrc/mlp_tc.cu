@@ -11,11 +11,7 @@
 //   * a layer is D[128 x N] = A[128 x K] * W^T with A (activations) and W
 //     (weights, N x K) in shared memory, issued as K/16 tcgen05.mma
 //     (kind::f16, bf16 x bf16 -> f32, M = 128) by one thread of the
-//     warpgroup and tracked by tcgen05.commit on the warpgroup's mbarriers;
-//     a hidden layer is issued as two N = 64 halves with a commit each
-//     (ordered so that no MMA still reads the activations the epilogue of
-//     the first half overwrites), so the epilogue starts on output columns
-//     0-63 while the tensor cores still compute part of columns 64-127;
+//     warpgroup and tracked by tcgen05.commit on the warpgroup's mbarrier;
 //   * the bias enters the accumulator through one more MMA per layer (see
 //     TcSmem), so the epilogue reads the pre-activation row of its voxel from
 //     TMEM (tcgen05.ld 32x32b), applies GELU and writes the bf16 row as the
@@ -72,7 +68,7 @@ struct __align__(1024) TcSmem {
   // activation tile (128 x 128); the first epilogue overwrites it only after
   // the layer-1 MMAs that read it have completed
   bf16 act[NWG][128 * HID];
-  unsigned long long mbar[NWG][2];  // per warpgroup: columns 0-63, 64-127 of a hidden layer
+  unsigned long long mbar[NWG];
   uint32_t tmem_base;
 };
 
@@ -166,8 +162,7 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
   }
   if (threadIdx.x == 0) {
     for (int i = 0; i < NWG; ++i)
-      for (int h = 0; h < 2; ++h)
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.mbar[i][h])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&S.mbar[i])) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -184,14 +179,13 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
   const uint32_t tbase = S.tmem_base;
   const uint32_t d_tmem = tbase + uint32_t(g * 128);                           // lane 0, this warpgroup's columns
   const uint32_t t_row = tbase + (uint32_t((warp & 3) * 32) << 16) + uint32_t(g * 128);  // this warp's lanes
-  const uint32_t mbar0 = smem_u32(&S.mbar[g][0]), mbar1 = smem_u32(&S.mbar[g][1]);
+  const uint32_t mbar = smem_u32(&S.mbar[g]);
   const uint32_t xs = smem_u32(S.act[g]), as = smem_u32(S.act[g]);
   const uint32_t w1s = smem_u32(S.w1), w2s = smem_u32(S.w2), w3s = smem_u32(S.w3), w4s = smem_u32(S.w4);
   const uint32_t ones_s = smem_u32(S.ones);
   const bool issuer = r == 0;
-  constexpr uint32_t ID_HALF = idesc_bf16(128, HID / 2), ID_OUT = idesc_bf16(128, NOUT_MMA);
-  uint32_t phase0 = 0, phase1 = 0;
-  bool pend1 = false;  // a commit on mbar1 not yet waited for (uniform over the warpgroup)
+  constexpr uint32_t ID_HID = idesc_bf16(128, HID), ID_OUT = idesc_bf16(128, NOUT_MMA);
+  uint32_t phase = 0;
   bool lost = false;
 
   const long long ntiles = (p.n + 127) / 128;
@@ -244,57 +238,25 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
       const bool skip = layer == 0 && tile == p.skip_tile;
       if (issuer && !skip) {
         fence_after_sync();
-        if (layer < 3) {
-          // A hidden layer as two N = 64 halves (output columns 64 h onward:
-          // weight rows 64 h onward, accumulator columns 64 h onward). The
-          // activations are updated in place, so the epilogue may overwrite
-          // input columns 0-63 only once no MMA still reads them: the MMAs of
-          // half 1 over input columns 0-63 go first, then all of half 0 and
-          // the first commit (mbar0), then the rest of half 1 (input columns
-          // 64-127) and its commit (mbar1). The epilogue of output columns
-          // 0-63 then runs while the tensor cores finish half 1.
-          const uint32_t bs = smem_u32(S.bias[layer]);
-          const uint32_t d0 = d_tmem, d1 = d_tmem + 64u;
-          if (layer == 0) {  // K = 16: one MMA per half, both before the first commit
-            mma_bf16(d1, smem_desc(xs, 128, 256), smem_desc(w1s + 2048, 128, 256), ID_HALF, 0u);
-            mma_bf16(d1, smem_desc(ones_s, 128, 256), smem_desc(bs + 2048, 128, 256), ID_HALF, 1u);
-            mma_bf16(d0, smem_desc(xs, 128, 256), smem_desc(w1s, 128, 256), ID_HALF, 0u);
-            mma_bf16(d0, smem_desc(ones_s, 128, 256), smem_desc(bs, 128, 256), ID_HALF, 1u);
-            mma_commit(mbar0);
-            mma_commit(mbar1);
-          } else {
-            const uint32_t ws = layer == 1 ? w2s : w3s;
-#pragma unroll
-            for (int kk = 0; kk < HID / 32; ++kk)  // half 1, input columns 0-63
-              mma_bf16(d1, smem_desc(as + kk * 256, 128, 2048), smem_desc(ws + 16384 + kk * 256, 128, 2048),
-                       ID_HALF, kk > 0 ? 1u : 0u);
-#pragma unroll
-            for (int kk = 0; kk < HID / 16; ++kk)  // half 0
-              mma_bf16(d0, smem_desc(as + kk * 256, 128, 2048), smem_desc(ws + kk * 256, 128, 2048), ID_HALF,
-                       kk > 0 ? 1u : 0u);
-            mma_bf16(d0, smem_desc(ones_s, 128, 256), smem_desc(bs, 128, 256), ID_HALF, 1u);
-            mma_commit(mbar0);
-#pragma unroll
-            for (int kk = HID / 32; kk < HID / 16; ++kk)  // half 1, input columns 64-127
-              mma_bf16(d1, smem_desc(as + kk * 256, 128, 2048), smem_desc(ws + 16384 + kk * 256, 128, 2048),
-                       ID_HALF, 1u);
-            mma_bf16(d1, smem_desc(ones_s, 128, 256), smem_desc(bs + 2048, 128, 256), ID_HALF, 1u);
-            mma_commit(mbar1);
-          }
+        if (layer == 0) {
+          mma_bf16(d_tmem, smem_desc(xs, 128, 256), smem_desc(w1s, 128, 256), ID_HID, 0u);
         } else {
+          const uint32_t ws = layer == 1 ? w2s : (layer == 2 ? w3s : w4s);
+          const uint32_t id = layer == 3 ? ID_OUT : ID_HID;
 #pragma unroll
           for (int kk = 0; kk < HID / 16; ++kk)
-            mma_bf16(d_tmem, smem_desc(as + kk * 256, 128, 2048), smem_desc(w4s + kk * 256, 128, 2048), ID_OUT,
+            mma_bf16(d_tmem, smem_desc(as + kk * 256, 128, 2048), smem_desc(ws + kk * 256, 128, 2048), id,
                      kk > 0 ? 1u : 0u);
-          mma_bf16(d_tmem, smem_desc(ones_s, 128, 256), smem_desc(smem_u32(S.bias4), 128, 256), ID_OUT, 1u);
-          mma_commit(mbar0);
         }
+        // + bias: ones (128 x 16) times the layer's bias terms (N x 16)
+        const uint32_t bs = layer < 3 ? smem_u32(S.bias[layer]) : smem_u32(S.bias4);
+        mma_bf16(d_tmem, smem_desc(ones_s, 128, 256), smem_desc(bs, 128, 256), layer == 3 ? ID_OUT : ID_HID, 1u);
+        mma_commit(mbar);
       }
-      pend1 = layer < 3 && !skip;
       // one warp polls the mbarrier; the other three wait in the hardware
       // barrier below and take no issue slots from the other tiles' epilogues
-      const bool ok = (warp & 3) != 0 || mbar_wait(mbar0, phase0, p.wait_limit);
-      phase0 ^= 1u;
+      const bool ok = (warp & 3) != 0 || mbar_wait(mbar, phase, p.wait_limit);
+      phase ^= 1u;
       if (wg_sync_any(g, !ok)) {
         lost = true;
         break;
@@ -302,35 +264,20 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
       fence_after_sync();
       if (layer < 3) {
         // 16 columns at a time, the next chunk's TMEM load in flight while
-        // this chunk's GELU runs; the second half after its own commit
+        // this chunk's GELU runs
         unsigned char* row_base = reinterpret_cast<unsigned char*>(S.act[g]) + core_off(r, 0, HID);
         uint32_t a0[16], a1[16];
+        tmem_ld16_start(t_row, a0);
+        tmem_wait16(a0);
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          if (h == 1) {
-            const bool ok1 = (warp & 3) != 0 || mbar_wait(mbar1, phase1, p.wait_limit);
-            phase1 ^= 1u;
-            pend1 = false;
-            if (wg_sync_any(g, !ok1)) {
-              lost = true;
-              break;
-            }
-            fence_after_sync();
-          }
-          const int c0 = h * 4;
-          tmem_ld16_start(t_row + uint32_t(c0 * 16), a0);
-          tmem_wait16(a0);
-#pragma unroll
-          for (int c = c0; c < c0 + 4; c += 2) {
-            tmem_ld16_start(t_row + uint32_t((c + 1) * 16), a1);
-            gelu_row16(a0, c * 16, row_base);
-            tmem_wait16(a1);
-            if (c + 2 < c0 + 4) tmem_ld16_start(t_row + uint32_t((c + 2) * 16), a0);
-            gelu_row16(a1, (c + 1) * 16, row_base);
-            if (c + 2 < c0 + 4) tmem_wait16(a0);
-          }
+        for (int c = 0; c < HID / 16; c += 2) {
+          tmem_ld16_start(t_row + uint32_t((c + 1) * 16), a1);
+          gelu_row16(a0, c * 16, row_base);
+          tmem_wait16(a1);
+          if (c + 2 < HID / 16) tmem_ld16_start(t_row + uint32_t((c + 2) * 16), a0);
+          gelu_row16(a1, (c + 1) * 16, row_base);
+          if (c + 2 < HID / 16) tmem_wait16(a0);
         }
-        if (lost) break;
       } else {
         float y[16];
         tmem_ld16(t_row, y);
@@ -349,11 +296,9 @@ __global__ void __launch_bounds__(THREADS, 1) mlp_infer_tc_kernel(const TcArgs p
     }
   }
   if (lost && issuer) {
-    // a lost phase may still complete: give the warpgroup's MMAs a second
-    // bounded wait on each barrier's last committed phase before the TMEM
-    // they write is returned (a completed phase returns at once)
-    (void)mbar_wait(mbar0, phase0 ^ 1u, p.wait_limit);
-    (void)mbar_wait(mbar1, pend1 ? phase1 : phase1 ^ 1u, p.wait_limit);
+    // the lost phase may still complete: give the warpgroup's MMAs a second
+    // bounded wait before the TMEM they write is returned
+    (void)mbar_wait(mbar, phase ^ 1u, p.wait_limit);
     if (p.status) atomicExch(p.status, 1);
   }
   // all TMEM reads done before the allocation is returned
