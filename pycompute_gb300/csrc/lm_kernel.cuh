@@ -671,23 +671,18 @@ template <typename TA, int M, int NC> struct RegConsts {
 struct NoEpilogue {
   template <class PArr, class DArr, class T>
   PCGB_HD void operator()(const PArr&, const DArr&, T) const {}
-  template <class DArr>
-  PCGB_HD void prologue(const DArr&) {}
   static constexpr bool kActive = false;
-  static constexpr bool kPrologue = false;
 };
 
 // All iterations of one voxel; then epi(p, d, fend) with the final parameters
 // and the samples still in registers and the cost at the final parameters
 // where the iterations evaluated it (NaN otherwise; see lm_iterate). A voxel
-// converged before the call loads p and d for the epilogue. An epilogue with
-// kPrologue also sees the samples before the iterations (epi.prologue(d)),
-// to compute what it needs from them alone while few registers are live.
+// converged before the call loads p and d for the epilogue.
 // With LANES > 1 the voxel's samples are split over LANES adjacent lanes
 // (lane `sub` of them; see lm_iterate) and lane 0 writes the results.
 template <class Model, int M, typename TA, typename TS, bool SHARED_C, bool SHARED_B, int LANES = 1,
           class Epi = NoEpilogue>
-PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, Epi epi = Epi{}, int sub = 0) {
+PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, const Epi& epi = Epi{}, int sub = 0) {
   static_assert(LANES == 1 || !Epi::kActive, "epilogues run with one lane per voxel");
   constexpr int P = Model::P, H = Model::H, C = Model::C, ML = lane_samples<M, LANES>();
   const long long N = a.N;
@@ -706,7 +701,6 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, Epi epi = Epi{}, i
       for (int k = 0; k < P; ++k) p[k] = load<TA>(a.pars, k * N + v);
 #pragma unroll
       for (int i = 0; i < M; ++i) d[i] = load<TA>(a.data, i * N + v);
-      if constexpr (Epi::kPrologue) epi.prologue(d);
       epi(p, d, Num<TA>::nan());
     }
     return;
@@ -730,7 +724,6 @@ PCGB_HD void lm_fit_voxel(const PcgbLmParams& a, long long v, Epi epi = Epi{}, i
 #pragma unroll
     for (int i = 0; i < C * M; ++i) cv[i] = load<TA>(a.consts, i * a.cstride + v);
   }
-  if constexpr (Epi::kPrologue) epi.prologue(d);
   TA lam = fresh ? TA(a.lam_start) : load<TA>(a.lam, v);
   int st = fresh ? 1 : a.step_type[v];
   TA f = fresh ? TA(0) : load<TA>(a.f, v);
@@ -1158,35 +1151,18 @@ __device__ void lm_check_grid(const PcgbLmParams& a) {
 // state reset as warm_check_voxel; the flagged voxels of each group of lanes
 // that reaches this point together are compacted with one atomic (any
 // grouping gives a valid list).
-// the plain fitter's constant start of a voxel (NaN entries: its largest sample)
-template <class Model, int M, typename TA>
-PCGB_HD void constant_start(const PcgbLmParams& a, const TA (&d)[M], TA (&p0)[Model::P]) {
-  TA mx = -Num<TA>::inf();
-#pragma unroll
-  for (int i = 0; i < M; ++i) mx = fmax(mx, d[i]);
-#pragma unroll
-  for (int k = 0; k < Model::P; ++k) p0[k] = isnan(a.init_val[k]) ? mx : TA(a.init_val[k]);
-}
-
-// the cost at the constant start (out of line, like warm_flag_voxel)
 template <class Model, int M, typename TA, bool SHARED_C>
-__device__ __noinline__ TA start_cost(const PcgbLmParams& a, long long v, const TA (&d)[M]) {
-  TA p0[Model::P];
-  constant_start<Model, M, TA>(a, d, p0);
-  return voxel_cost<Model, M, TA, SHARED_C>(a, v, p0, d);
-}
-
-// c0: the cost at the constant start. Kept out of line: called once per voxel
-// after its iterations, its temporaries then do not compete with the
-// iteration loop's registers.
-template <class Model, int M, typename TA, bool SHARED_C>
-__device__ __noinline__ void warm_flag_voxel(const PcgbLmParams& a, long long v, const TA (&p)[Model::P],
-                                             const TA (&d)[M], TA c, TA c0) {
+__device__ void warm_flag_voxel(const PcgbLmParams& a, long long v, const TA (&p)[Model::P], const TA (&d)[M], TA c) {
   constexpr int P = Model::P;
   const long long N = a.N;
   if (a.iters == 0) c = voxel_cost<Model, M, TA, SHARED_C>(a, v, p, d);
   TA p0[P];
-  constant_start<Model, M, TA>(a, d, p0);
+  TA mx = -Num<TA>::inf();
+#pragma unroll
+  for (int i = 0; i < M; ++i) mx = fmax(mx, d[i]);
+#pragma unroll
+  for (int k = 0; k < P; ++k) p0[k] = isnan(a.init_val[k]) ? mx : TA(a.init_val[k]);
+  const TA c0 = voxel_cost<Model, M, TA, SHARED_C>(a, v, p0, d);
   bool flag = !isfinite(c) || !(c < c0);
 #pragma unroll
   for (int k = 0; k < P; ++k) {
@@ -1221,12 +1197,9 @@ template <class Model, int M, typename TA, bool SHARED_C>
 struct FlagEpilogue {
   const PcgbLmParams& a;
   long long v;
-  TA c0 = TA(0);  // cost at the constant start, from the prologue
   static constexpr bool kActive = true;
-  static constexpr bool kPrologue = true;
-  PCGB_HD void prologue(const TA (&d)[M]) { c0 = start_cost<Model, M, TA, SHARED_C>(a, v, d); }
   PCGB_HD void operator()(const TA (&p)[Model::P], const TA (&d)[M], TA c) const {
-    warm_flag_voxel<Model, M, TA, SHARED_C>(a, v, p, d, c, c0);
+    warm_flag_voxel<Model, M, TA, SHARED_C>(a, v, p, d, c);
   }
 };
 
@@ -1301,8 +1274,6 @@ struct SelectEpilogue {
   const PcgbLmParams& a;
   long long i, v;
   static constexpr bool kActive = true;
-  static constexpr bool kPrologue = false;
-  PCGB_HD void prologue(const TA (&)[M]) {}
   PCGB_HD void operator()(const TA (&p)[Model::P], const TA (&d)[M], TA) const {
     warm_select_voxel<Model, M, TA, SHARED_C>(a, i, v, p, d);
   }
