@@ -79,10 +79,11 @@ NET_FLOP_PER_VOXEL = 2 * (16 * 128 + 2 * 128 * 128 + 128 * 4)
 # Binding-unit work per unit, from ncu opcode counts (sass__inst_executed per
 # opcode over one launch, divided by the units it processed): FP64-pipe
 # instructions (56 DFMA + 24 DMUL + 2 DADD) per IVIM-16 voxel-iteration of the
-# FP64-solve LM (4,194,304 warm-started voxels x 2 iterations) and MUFU
-# instructions per voxel of the tcgen05 network (1,048,576 IVIM-16 voxels).
+# FP64-solve warm LM (4,194,304 warm-started voxels x 3 iterations) and MUFU
+# instructions per voxel of the tcgen05 network (1,048,576 IVIM-16 voxels;
+# 240 tanh for the 240 activations of the tanh columns, 16 log, 3 exp/rcp).
 FP64_OPS_PER_VOXEL_ITER = 82
-MUFU_PER_VOXEL_NET = 403
+MUFU_PER_VOXEL_NET = 259
 # issue rates per SM per clock on sm_103a: FP64 at 1/64 of the 128 FP32 lanes,
 # MUFU 16 lanes
 FP64_PER_SM_CLK = 2

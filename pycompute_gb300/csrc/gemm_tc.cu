@@ -90,14 +90,23 @@ __device__ __forceinline__ void stage(bf16* dst, const bf16* src, long long ld, 
       *reinterpret_cast<uint4*>(base + core_off(r, kc, BK)) = v;
     }
   } else {
-    // BK x (ROWS / 8) chunks of 8 row-values, scattered into their rows
-    for (int c = threadIdx.x; c < BK * (ROWS / 8); c += THREADS) {
-      const int kr = c / (ROWS / 8), rc = (c % (ROWS / 8)) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (r0 + rc < rows_live && k0 + kr < kend) v = *reinterpret_cast<const uint4*>(src + (k0 + kr) * ld + r0 + rc);
-      const unsigned short* e = reinterpret_cast<const unsigned short*>(&v);
+    // (BK / 2) x (ROWS / 8) pairs of chunks: rows k, k + 1 (k even) of 8
+    // row-values each, scattered into their rows as 32-bit words (element k
+    // and k + 1 of a row are adjacent in the layout); k varies fastest across
+    // a warp, which spreads the words over more banks. Both rows of a pair are
+    // inside or outside the K range together (it is a multiple of 8).
+    for (int c = threadIdx.x; c < (BK / 2) * (ROWS / 8); c += THREADS) {
+      const int kr = (c % (BK / 2)) * 2, rc = (c / (BK / 2)) * 8;
+      uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
+      if (r0 + rc < rows_live && k0 + kr < kend) {
+        v0 = *reinterpret_cast<const uint4*>(src + (k0 + kr) * ld + r0 + rc);
+        v1 = *reinterpret_cast<const uint4*>(src + (k0 + kr + 1) * ld + r0 + rc);
+      }
+      const unsigned short* e0 = reinterpret_cast<const unsigned short*>(&v0);
+      const unsigned short* e1 = reinterpret_cast<const unsigned short*>(&v1);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) *reinterpret_cast<unsigned short*>(base + core_off(rc + q, kr, BK)) = e[q];
+      for (int q = 0; q < 8; ++q)
+        *reinterpret_cast<uint32_t*>(base + core_off(rc + q, kr, BK)) = uint32_t(e0[q]) | (uint32_t(e1[q]) << 16);
     }
   }
 }
