@@ -241,14 +241,19 @@ class WarmStartMLP:
             b1, b2 = 0.9, 0.999
             graph = None
             total = epochs * nb
+            # per step: Adam's two bias corrections and the cosine-decay scale,
+            # made once and read from device memory (no host copy per step, so
+            # the host queues steps ahead of the device)
+            steps = [self.step + 1 + i for i in range(total)]
+            corr_tab = torch.tensor([[1 - b1 ** s, 1 - b2 ** s, 0.5 * (1.0 + np.cos(np.pi * i / total))]
+                                     for i, s in enumerate(steps)], dtype=torch.float32).to(self.device)
             done = 0
             for ep in range(epochs):
                 for b in range(nb):
                     self.bx.copy_(x[b * batch:(b + 1) * batch])
                     self.bt.copy_(t[b * batch:(b + 1) * batch])
                     self.step += 1
-                    scale = 0.5 * (1.0 + np.cos(np.pi * done / total))  # cosine decay
-                    self.corr.copy_(torch.tensor([1 - b1 ** self.step, 1 - b2 ** self.step, scale]))
+                    self.corr.copy_(corr_tab[done])
                     if not use_graph or done == 0:
                         # the first step runs eagerly so every kernel is loaded before capture
                         self._train_step_launches(lr, k_split)
