@@ -839,19 +839,26 @@ def mixed_batch_comparison(n_per_model=1 << 20, iters=100, seed=300):
         acc[w.name] = {"median_rel_err": med, "frac_voxels_gt_1e-4": frac,
                        "per_param_median": _per_param_median(j.pars, p64)}
         # the model's own 1e-4 budget: error against the converged all-FP64
-        # fit (300 iterations, tol 1e-30) of the fp32 fitter at growing budgets
+        # fit (300 iterations, tol 1e-30) of the fp32 fitter at growing
+        # budgets, once with the batch's convergence tolerance (1e-8: the
+        # projected-gradient test on unscaled parameters stops a voxel whose
+        # cost is flat in one parameter, e.g. T1 in ms, before that parameter
+        # settles) and once with tol 1e-30 like the reference fit (every
+        # budget iteration runs: the error left is the fp32 fitter's own)
         s64.setup(p64.copy_(i0.double()), list(w.protocol), j.data.double(), list(w.lb), list(w.ub))
         s64.run(300, tol=1e-30)
         s32 = SecondOrderLevenbergMarquardt(Expr(w.expr, w.pars, w.consts), None, w.M, torch.float32)
-        curve, k_tol = {}, None
-        for k in (25, 50, 100, 200, 400):
-            p32 = i0.clone()
-            s32.setup(p32, list(w.protocol), j.data, list(w.lb), list(w.ub))
-            s32.run(k)
-            curve[k] = _median_rel_gpu(p32, p64)[0]
-            if k_tol is None and curve[k] <= TOL:
-                k_tol = k
-        acc[w.name]["vs_fp64_converged"] = {"median_rel_err_by_iters": curve, "iters_for_1e-4": k_tol}
+        for key, tol in (("vs_fp64_converged", 1e-8), ("vs_fp64_converged_tol_1e-30", 1e-30)):
+            curve, k_tol = {}, None
+            for k in (25, 50, 100, 200, 400):
+                p32 = i0.clone()
+                s32.setup(p32, list(w.protocol), j.data, list(w.lb), list(w.ub))
+                s32.run(k, tol=tol)
+                curve[k] = _median_rel_gpu(p32, p64)[0]
+                if k_tol is None and curve[k] <= TOL:
+                    k_tol = k
+            acc[w.name][key] = {"tol": tol, "median_rel_err_by_iters": curve, "iters_for_1e-4": k_tol,
+                                "per_param_median_at_400": _per_param_median(p32, p64)}
         del s64, p64, s32
     return {"workload": "mixed_vfa8_t2s16_ivim10_biexp32", "voxels": total, "iters": iters,
             "autotuned": {k: tuned.get(k) for k in ("block", "maxrreg", "chunk", "order", "lanes", "ms")},

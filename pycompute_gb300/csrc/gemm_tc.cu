@@ -9,15 +9,19 @@
 //   a_layout 0: A stored (M, K) row-major (K-major), 1: (K, M) row-major
 //   b_layout 0: B stored (N, K) row-major (K-major), 1: (K, N) row-major
 //
-// One CTA of 128 threads computes a 128 x 64 tile of C over its K range
-// (blockIdx.z selects the split-K range). Per 32-wide K step the threads stage
-// both operand tiles into shared memory in the canonical K-major core-matrix
-// layout (a transposed operand is scattered element by element while staging,
-// so every MMA reads the layout the inference kernel uses), and one thread
-// issues two tcgen05.mma (M = 128, N = 64, K = 16) into the 64 accumulator
-// columns and commits them to the stage's mbarrier; two stages alternate, so
-// staging step t + 1 overlaps the MMAs of step t. The epilogue reads row r of
-// the accumulator (thread r = TMEM lane r) with tcgen05.ld. Every mbarrier
+// One CTA of 128 threads computes a 128 x 32 tile of C over its K range
+// (blockIdx.z selects the split-K range); the narrow tile doubles the CTAs of
+// the training step's small GEMMs and halves each thread's epilogue, which
+// bounds their latency. Per 32-wide K step the threads stage both operand
+// tiles into shared memory in the canonical K-major core-matrix layout (a
+// transposed operand is scattered as 32-bit pairs while staging, so every MMA
+// reads the layout the inference kernel uses), and one thread issues two
+// tcgen05.mma (M = 128, N = 32, K = 16) into the 32 accumulator columns and
+// commits them to the stage's mbarrier; two stages alternate, and
+// the global loads of step t + 1 are in flight while step t is staged and its
+// MMAs issue. The epilogue reads row r of the accumulator (thread r = TMEM
+// lane r) with tcgen05.ld and passes each warp's rows through shared memory,
+// so its global stores, loads and atomics are row-contiguous. Every mbarrier
 // wait is bounded: on timeout the CTA records the loss in *status, waits once
 // more (bounded) for its MMAs in flight, skips its epilogue and still frees
 // its tensor memory.
@@ -36,12 +40,12 @@ namespace pcgb_gemm_tc {
 using pcgb_mlp::bf16;
 using namespace pcgb_tc;
 
-constexpr int BM = 128, BN = 64, BK = 32;
+constexpr int BM = 128, BN = 32, BK = 32;
 constexpr int THREADS = 128;
-constexpr int TMEM_COLS = 64;
+constexpr int TMEM_COLS = 32;  // BN fp32 accumulator columns (the minimum allocation)
 constexpr unsigned kWaitLimit = 1u << 22;
 // dynamic shared memory requested per CTA: at most 7 CTAs fit on an SM, so
-// their 7 x 64 accumulator columns never exceed the SM's 512 and no
+// their 7 x 32 accumulator columns never exceed the SM's 512 and no
 // tcgen05.alloc has to wait for another CTA
 constexpr int kSmemBytes = 32 * 1024;
 
@@ -73,49 +77,90 @@ struct __align__(1024) GemmSmem {
 };
 static_assert(sizeof(GemmSmem) <= kSmemBytes && kSmemBytes <= 48 * 1024, "GEMM shared memory");
 
-// Stage the rows x BK tile at (r0, k0) of an operand into the canonical
-// K-major layout. KMAJOR: element (r, k) at src[r * ld + k], else at
-// src[k * ld + r]. Rows >= rows_live are loaded when the stored row is long
-// enough (their results are masked); columns at or past kend are zero.
+// One operand's rows x BK tile at (r0, k0), held in registers between its
+// global loads and its shared-memory stores, so the loads of step t + 1 are
+// in flight while step t is staged and its MMAs issue. KMAJOR: element (r, k)
+// at src[r * ld + k], else at src[k * ld + r]. Rows >= rows_live are loaded
+// when the stored row is long enough (their results are masked); columns at
+// or past kend are zero. Stores go to the canonical K-major layout.
 template <int ROWS, bool KMAJOR>
-__device__ __forceinline__ void stage(bf16* dst, const bf16* src, long long ld, long long r0, long long rows_live,
-                                      long long k0, long long kend) {
-  unsigned char* base = reinterpret_cast<unsigned char*>(dst);
-  if (KMAJOR) {
-    // ROWS x (BK / 8) chunks of 8 k-values
-    for (int c = threadIdx.x; c < ROWS * (BK / 8); c += THREADS) {
-      const int r = c / (BK / 8), kc = (c % (BK / 8)) * 8;
-      uint4 v = make_uint4(0, 0, 0, 0);
-      if (r0 + r < rows_live && k0 + kc < kend) v = *reinterpret_cast<const uint4*>(src + (r0 + r) * ld + k0 + kc);
-      *reinterpret_cast<uint4*>(base + core_off(r, kc, BK)) = v;
-    }
-  } else {
-    // (BK / 2) x (ROWS / 8) pairs of chunks: rows k, k + 1 (k even) of 8
-    // row-values each, scattered into their rows as 32-bit words (element k
-    // and k + 1 of a row are adjacent in the layout); k varies fastest across
-    // a warp, which spreads the words over more banks. Both rows of a pair are
-    // inside or outside the K range together (it is a multiple of 8).
-    for (int c = threadIdx.x; c < (BK / 2) * (ROWS / 8); c += THREADS) {
-      const int kr = (c % (BK / 2)) * 2, rc = (c / (BK / 2)) * 8;
-      uint4 v0 = make_uint4(0, 0, 0, 0), v1 = v0;
-      if (r0 + rc < rows_live && k0 + kr < kend) {
-        v0 = *reinterpret_cast<const uint4*>(src + (k0 + kr) * ld + r0 + rc);
-        v1 = *reinterpret_cast<const uint4*>(src + (k0 + kr + 1) * ld + r0 + rc);
-      }
-      const unsigned short* e0 = reinterpret_cast<const unsigned short*>(&v0);
-      const unsigned short* e1 = reinterpret_cast<const unsigned short*>(&v1);
+struct OperandTile {
+  // KMAJOR: ROWS x (BK / 8) chunks of 8 k-values; else (BK / 2) x (ROWS / 8)
+  // pairs of chunks (rows k, k + 1 of 8 row-values each)
+  static constexpr int kItems = KMAJOR ? ROWS * (BK / 8) : (BK / 2) * (ROWS / 8);
+  static constexpr int kPer = (kItems + THREADS - 1) / THREADS;
+  static_assert(kItems % THREADS == 0 || kPer == 1, "operand tile items per thread");
+  // threads past the last item (kItems < THREADS) load and store nothing
+  static __device__ __forceinline__ bool mine(int c) { return kItems % THREADS == 0 || c < kItems; }
+  uint4 v[KMAJOR ? kPer : 2 * kPer];
+
+  __device__ __forceinline__ void load(const bf16* src, long long ld, long long r0, long long rows_live,
+                                       long long k0, long long kend) {
 #pragma unroll
-      for (int q = 0; q < 8; ++q)
-        *reinterpret_cast<uint32_t*>(base + core_off(rc + q, kr, BK)) = uint32_t(e0[q]) | (uint32_t(e1[q]) << 16);
+    for (int i = 0; i < kPer; ++i) {
+      const int c = threadIdx.x + i * THREADS;
+      if (!mine(c)) break;
+      if (KMAJOR) {
+        const int r = c / (BK / 8), kc = (c % (BK / 8)) * 8;
+        v[i] = make_uint4(0, 0, 0, 0);
+        if (r0 + r < rows_live && k0 + kc < kend) v[i] = *reinterpret_cast<const uint4*>(src + (r0 + r) * ld + k0 + kc);
+      } else {
+        // k varies fastest across a warp (spreads the scattered words over
+        // more banks); both rows of a pair are inside or outside the K range
+        // together (it is a multiple of 8)
+        const int kr = (c % (BK / 2)) * 2, rc = (c / (BK / 2)) * 8;
+        v[2 * i] = make_uint4(0, 0, 0, 0);
+        v[2 * i + 1] = v[2 * i];
+        if (r0 + rc < rows_live && k0 + kr < kend) {
+          v[2 * i] = *reinterpret_cast<const uint4*>(src + (k0 + kr) * ld + r0 + rc);
+          v[2 * i + 1] = *reinterpret_cast<const uint4*>(src + (k0 + kr + 1) * ld + r0 + rc);
+        }
+      }
     }
   }
-}
+
+  __device__ __forceinline__ void store(bf16* dst) const {
+    unsigned char* base = reinterpret_cast<unsigned char*>(dst);
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int c = threadIdx.x + i * THREADS;
+      if (!mine(c)) break;
+      if (KMAJOR) {
+        const int r = c / (BK / 8), kc = (c % (BK / 8)) * 8;
+        *reinterpret_cast<uint4*>(base + core_off(r, kc, BK)) = v[i];
+      } else {
+        // element k and k + 1 of a row are adjacent in the layout: one 32-bit
+        // word per row of the chunk
+        const int kr = (c % (BK / 2)) * 2, rc = (c / (BK / 2)) * 8;
+        const unsigned short* e0 = reinterpret_cast<const unsigned short*>(&v[2 * i]);
+        const unsigned short* e1 = reinterpret_cast<const unsigned short*>(&v[2 * i + 1]);
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+          *reinterpret_cast<uint32_t*>(base + core_off(rc + q, kr, BK)) = uint32_t(e0[q]) | (uint32_t(e1[q]) << 16);
+      }
+    }
+  }
+};
+
+// Epilogue staging, one region per warp, laid over the operand buffers once
+// every MMA has completed: a warp's 32 accumulator rows (one per thread) are
+// written row-wise and read back column-wise, so the global stores, loads and
+// atomics of a 16-column chunk touch two 64-byte row segments per
+// instruction instead of 32 rows.
+constexpr int kEpiPitch = 17;  // floats per staged row: odd, so the row-per-thread writes hit distinct banks
+struct EpiStage {
+  // fp32 outputs, or (GELU' epilogue, which stores no fp32) the
+  // pre-activations it reads
+  float f[THREADS / 32][32 * kEpiPitch];
+  uint32_t h[THREADS / 32][32 * 9];         // bf16 outputs, as pairs (8 words per row + 1 pad)
+};
+static_assert(sizeof(EpiStage) <= sizeof(bf16) * 2 * (BM + BN) * BK, "epilogue staging fits the operand buffers");
 
 template <bool A_ROW, bool B_NK, int EPI>
 __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   GemmSmem& S = *reinterpret_cast<GemmSmem*>(smem_raw);
-  const int warp = threadIdx.x >> 5;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long m0 = (long long)blockIdx.y * BM, n0 = (long long)blockIdx.x * BN;
   const long long kbeg = (long long)blockIdx.z * g.k_split;
   const long long kend = kbeg + g.k_split < g.K ? kbeg + g.k_split : g.K;
@@ -131,6 +176,12 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
                  "r"(TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  OperandTile<BM, A_ROW> ta;
+  OperandTile<BN, B_NK> tb;
+  if (steps > 0) {
+    ta.load(g.A, g.lda, m0, g.M, kbeg, kend);
+    tb.load(g.B, g.ldb, n0, g.N, kbeg, kend);
   }
   fence_before_sync();
   __syncthreads();
@@ -149,9 +200,13 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
         break;
       }
     }
-    const long long k0 = kbeg + (long long)t * BK;
-    stage<BM, A_ROW>(S.a[buf], g.A, g.lda, m0, g.M, k0, kend);
-    stage<BN, B_NK>(S.b[buf], g.B, g.ldb, n0, g.N, k0, kend);
+    ta.store(S.a[buf]);
+    tb.store(S.b[buf]);
+    if (t + 1 < steps) {
+      const long long k1 = kbeg + (long long)(t + 1) * BK;
+      ta.load(g.A, g.lda, m0, g.M, k1, kend);
+      tb.load(g.B, g.ldb, n0, g.N, k1, kend);
+    }
     fence_async_smem();  // staged operands -> visible to the tensor cores
     fence_before_sync();
     __syncthreads();
@@ -181,11 +236,19 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
     }
   } else {
     fence_after_sync();
-    const int r = threadIdx.x;  // accumulator row = TMEM lane
-    const long long m = m0 + r;
+    // every MMA has completed (or none ran): the operand buffers are free
+    EpiStage& E = *reinterpret_cast<EpiStage*>(smem_raw);
+    float* sf = E.f[warp];
+    float* sz = E.f[warp];
+    uint32_t* sh = E.h[warp];
+    const long long mw = m0 + warp * 32;  // first row of this warp = its TMEM lane quarter
     const uint32_t trow = tbase + (uint32_t(warp * 32) << 16);
+    constexpr bool kF32 = EPI != EPI_BWD_DGELU;
+    constexpr bool kBf16 = EPI == EPI_FWD_GELU || EPI == EPI_BWD_DGELU;
 #pragma unroll
     for (int c0 = 0; c0 < BN; c0 += 16) {
+      const long long nc = n0 + c0;
+      if (nc >= g.N) break;  // uniform over the CTA
       float v[16];
       if (steps > 0) {
         tmem_ld16(trow + uint32_t(c0), v);
@@ -193,27 +256,71 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) v[i] = 0.f;
       }
-      if (m >= g.M) continue;
+      if (EPI == EPI_BWD_DGELU) {
+        // the chunk's pre-activations, read row segment by row segment
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const long long n = n0 + c0 + i;
-        if (n >= g.N) break;
-        const float acc = v[i];
+        for (int j = 0; j < 16; ++j) {
+          const int idx = j * 32 + lane, rr = idx >> 4, cc = idx & 15;
+          const long long m = mw + rr, n = nc + cc;
+          sz[rr * kEpiPitch + cc] = (m < g.M && n < g.N) ? g.zin[m * g.ldz + n] : 0.f;
+        }
+        __syncwarp();
+      }
+      // column nc + i has i = its position modulo 16 (nc is a multiple of 16),
+      // so each pair's GELU recipe is fixed at compile time
+#pragma unroll
+      for (int i = 0; i < 16; i += 2) {
+        float o0 = v[i], o1 = v[i + 1];
+        uint32_t hb = 0;
+        if (EPI == EPI_FWD_GELU || EPI == EPI_FWD_LINEAR) {
+          o0 += nc + i < g.N ? g.bias[(nc + i) * g.bias_stride] : 0.f;
+          o1 += nc + i + 1 < g.N ? g.bias[(nc + i + 1) * g.bias_stride] : 0.f;
+        }
         if (EPI == EPI_FWD_GELU) {
-          const float z = acc + g.bias[n * g.bias_stride];
-          g.out_f32[m * g.ldo + n] = z;
-          g.out_bf16[m * g.ldob + n] = __float2bfloat16_rn(pcgb_mlp::gelu_col(z, int(n)));
-        } else if (EPI == EPI_FWD_LINEAR) {
-          g.out_f32[m * g.ldo + n] = acc + g.bias[n * g.bias_stride];
+          // gelu = (2 gelu) / 2, exact in bf16
+          const float2 t = __bfloat1622float2(pcgb_mlp::bits_bf162(pcgb_mlp::gelu2x_col_pack_bf16(o0, o1, i)));
+          hb = pcgb_mlp::pack_bf16(0.5f * t.x, 0.5f * t.y);
         } else if (EPI == EPI_BWD_DGELU) {
-          g.out_bf16[m * g.ldob + n] =
-              __float2bfloat16_rn(acc * pcgb_mlp::gelu_grad_col(g.zin[m * g.ldz + n], int(n)));
-        } else if (EPI == EPI_DW_ATOMIC) {
-          atomicAdd(&g.out_f32[m * g.ldo + n], acc);
-        } else {
-          g.out_f32[m * g.ldo + n] = acc;
+          hb = pcgb_mlp::pack_bf16(o0 * pcgb_mlp::gelu_grad_col(sz[lane * kEpiPitch + i], i),
+                                   o1 * pcgb_mlp::gelu_grad_col(sz[lane * kEpiPitch + i + 1], i + 1));
+        }
+        if (kF32) {
+          sf[lane * kEpiPitch + i] = o0;
+          sf[lane * kEpiPitch + i + 1] = o1;
+        }
+        if (kBf16) sh[lane * 9 + i / 2] = hb;
+      }
+      __syncwarp();
+      if (kF32) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int idx = j * 32 + lane, rr = idx >> 4, cc = idx & 15;
+          const long long m = mw + rr, n = nc + cc;
+          if (m < g.M && n < g.N) {
+            const float val = sf[rr * kEpiPitch + cc];
+            if (EPI == EPI_DW_ATOMIC) atomicAdd(&g.out_f32[m * g.ldo + n], val);
+            else g.out_f32[m * g.ldo + n] = val;
+          }
         }
       }
+      if (kBf16) {
+        // 32 rows x 8 words; ldob is even, so a pair at an even column is one
+        // aligned 32-bit word
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int idx = j * 32 + lane, rr = idx >> 3, w = idx & 7;
+          const long long m = mw + rr, n = nc + 2 * w;
+          if (m < g.M && n < g.N) {
+            const uint32_t pair = sh[rr * 9 + w];
+            if (n + 1 < g.N) {
+              *reinterpret_cast<uint32_t*>(g.out_bf16 + m * g.ldob + n) = pair;
+            } else {
+              g.out_bf16[m * g.ldob + n] = __ushort_as_bfloat16(uint16_t(pair & 0xffffu));
+            }
+          }
+        }
+      }
+      __syncwarp();  // the next chunk reuses the staging
     }
   }
   fence_before_sync();
@@ -276,6 +383,9 @@ int pcgb_gemm_bf16_tc(int a_layout, int b_layout, int epilogue, const void* A, i
   if (!out_f32 && epilogue != EPI_BWD_DGELU) return fail(PCGB_EINVAL, "out_f32 is required");
   if ((epilogue == EPI_FWD_GELU || epilogue == EPI_BWD_DGELU) && !out_bf16)
     return fail(PCGB_EINVAL, "out_bf16 is required");
+  if ((epilogue == EPI_FWD_GELU || epilogue == EPI_BWD_DGELU) &&
+      (ldob % 2 || reinterpret_cast<uintptr_t>(out_bf16) % 4))
+    return fail(PCGB_EINVAL, "out_bf16 must be 4-byte aligned with an even ldob");
   if (need_bias && !bias) return fail(PCGB_EINVAL, "bias is required");
   if (epilogue == EPI_BWD_DGELU && !zin) return fail(PCGB_EINVAL, "zin is required");
   if (M == 0 || N == 0) return PCGB_OK;
