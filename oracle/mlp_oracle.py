@@ -69,30 +69,27 @@ def _gelu_tanh_grad(z):
 
 
 # The polynomial recipe of the columns n with n % 16 < POLY_COLS (the GPU's
-# FMA-pipe GELU): 2 gelu(z) ~ (z + relu(|z| - 3)) + w e(w), w = min(z^2, 9),
-# e(w) = q1 + w (q2 + w (q3 + w q4)), the last step one fused multiply-add,
-# every operation in f16 with one rounding (products of f16 values and their
-# sums are exact in float64, so rounding the float64 result once to f16 is the
-# fused operation's rounding), then the f16 result rounded to bf16.
+# FMA-pipe GELU): 2 gelu(z) ~ 2 relu(z) + (w e(w) - a), a = min(|z|, 3),
+# w = a^2, e(w) = q1 + w (q2 + w (q3 + w q4)), every operation in bf16 with one
+# rounding (products of bf16 values and the sums formed here are exact in
+# float64 wherever the rounding to bf16 can depend on them, so rounding the
+# float64 result once to bf16 is the fused operation's rounding).
 POLY_COLS = 6
-_Q = (0.7880859375, -0.11566162109375, 0.0112457275390625, -0.0004475116729736328)
-
-
-def _f16(x):
-    with np.errstate(over="ignore", invalid="ignore"):
-        return np.asarray(x, dtype=np.float64).astype(np.float16).astype(np.float64)
+_Q = (0.7890625, -0.11572265625, 0.01116943359375, -0.0004405975341796875)
 
 
 def _gelu_poly(z):
-    zh = _f16(np.asarray(z, dtype=np.float32).astype(np.float64))
+    B = bf16_exact
+    zb = bf16(np.asarray(z, dtype=np.float32))
     with np.errstate(over="ignore", invalid="ignore"):
-        w = np.fmin(_f16(zh * zh), 9.0)
-        e = _f16(_Q[3] * w + _Q[2])
-        e = _f16(e * w + _Q[1])
-        e = _f16(e * w + _Q[0])
-        s = _f16(zh + np.maximum(_f16(np.abs(zh) - 3.0), 0.0))
-        g = _f16(e * w + s)
-        return 0.5 * bf16_exact(g)
+        a = np.fmin(np.abs(zb), 3.0)
+        w = B(a * a)
+        e = B(_Q[3] * w + _Q[2])
+        e = B(e * w + _Q[1])
+        e = B(e * w + _Q[0])
+        t = B(e * w - a)
+        r2 = np.maximum(B(2.0 * zb), 0.0)
+        return 0.5 * B(r2 + t)
 
 
 def _gelu_poly_grad(z):

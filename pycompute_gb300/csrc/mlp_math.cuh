@@ -57,40 +57,42 @@ __device__ __forceinline__ float gelu_grad(float z) {
 // above takes the MUFU pipe (two MUFU operations per pair of activations,
 // 16 per SM per clock); the network's columns n with n % 16 < kPolyCols
 // instead evaluate the same GELU with no MUFU operation, by a polynomial in
-// f16x2 arithmetic:
-//   2 gelu(z) ~ (z + relu(|z| - a)) + w e(w),  w = min(z^2, a^2),  a = 3,
-//   e(w) = q1 + w (q2 + w (q3 + w q4)),  w e(w) ~ z tanh(u(z)) on |z| <= a,
-// with z rounded to f16, every operation rounded once to f16 (the last one a
-// fused multiply-add; the product and sum use the non-contracting forms, so
-// the compiler cannot fuse them differently), then the f16 result rounded to
-// bf16. q1..q4 are a near-minimax fit of
-// z tanh(u(z)) in w = z^2 on [0, 9], weighted by 1/|z| (Lawson's iteratively
-// reweighted least squares, C. L. Lawson 1961), rounded to f16 and adjusted
-// by single f16 ulps to minimise the maximum error of the whole recipe; its
-// error is at most 0.0126 |z| (the MUFU recipe's at most 0.0176 |z|) for
-// |z| < 32752 (beyond, the f16 sum overflows). The columns are fixed, so
-// training and inference see the same activation per unit.
+// bf16x2 arithmetic:
+//   2 gelu(z) ~ 2 relu(z) + (w e(w) - a),  a = min(|z|, 3),  w = a^2,
+//   e(w) = q1 + w (q2 + w (q3 + w q4)),  w e(w) ~ |z| tanh(u(|z|)) on [0, 3],
+// which is z exactly where |z| <= 3 apart from w e(w) - |z| ~ z tanh(u) - |z|,
+// and 2 relu(z) - 0.011 beyond. Every operation is one bf16 rounding (fused
+// multiply-adds for the Horner steps and for w e - a, the non-contracting
+// forms for the product and the final sum, so the compiler cannot fuse them
+// differently); the small term w e - a is formed before it is added to
+// 2 relu(z), so large z see one rounding. Nine instructions per pair, the
+// result already the bf16 pair the next layer reads. q1..q4 are a
+// near-minimax fit of |z| tanh(u(|z|)) / w in w on [0, 9], weighted by |z|
+// (Lawson's iteratively reweighted least squares, C. L. Lawson 1961), rounded
+// to bf16 and adjusted by single bf16 ulps to minimise the maximum error of
+// the whole recipe over every bf16 input: at most 0.0110 |z| on bf16 z and
+// 0.0176 |z| on fp32 z, which adds z's rounding (the MUFU recipe: 0.0103 and
+// 0.0177 |z|). The columns are fixed, so training and inference see the same
+// activation per unit.
 constexpr int kPolyCols = 6;
 __device__ __forceinline__ bool poly_col(int n) { return (n & 15) < kPolyCols; }
-__device__ __forceinline__ __half2 h2bits(uint32_t v) { return *reinterpret_cast<__half2*>(&v); }
 __device__ __forceinline__ uint32_t gelu2x_poly_pack_bf16(float z0, float z1) {
-  const __half2 q1 = h2bits(0x3a4e3a4eu), q2 = h2bits(0xaf67af67u), q3 = h2bits(0x21c221c2u),
-                q4 = h2bits(0x8f558f55u);
-  const __half2 a2 = h2bits(0x48804880u), one = h2bits(0x3c003c00u), neg_a = h2bits(0xc200c200u);
-  const __half2 zh = __floats2half2_rn(z0, z1);
-  const __half2 w = __hmin2(__hmul2_rn(zh, zh), a2);
-  __half2 e = __hfma2(q4, w, q3);
+  const __nv_bfloat162 q1 = bits_bf162(0x3f4a3f4au), q2 = bits_bf162(0xbdedbdedu), q3 = bits_bf162(0x3c373c37u),
+                       q4 = bits_bf162(0xb9e7b9e7u);
+  const __nv_bfloat162 three = bits_bf162(0x40404040u), two = bits_bf162(0x40004000u), zero = bits_bf162(0u);
+  const __nv_bfloat162 z = __floats2bfloat162_rn(z0, z1);
+  const __nv_bfloat162 a = __hmin2(__habs2(z), three);
+  const __nv_bfloat162 w = __hmul2_rn(a, a);
+  __nv_bfloat162 e = __hfma2(q4, w, q3);
   e = __hfma2(e, w, q2);
   e = __hfma2(e, w, q1);
-  const __half2 s = __hadd2_rn(zh, __hfma2_relu(__habs2(zh), one, neg_a));
-  const float2 g = __half22float2(__hfma2(e, w, s));
-  return pack_bf16(g.x, g.y);
+  const __nv_bfloat162 t = __hfma2(e, w, __hneg2(a));
+  return bf162_bits(__hadd2_rn(__hfma2_relu(z, two, zero), t));
 }
 // d gelu / dz of the polynomial recipe (fp32, exact derivative of the
 // continuous form)
 __device__ __forceinline__ float gelu_poly_grad(float z) {
-  const float q1 = 0.7880859375f, q2 = -0.11566162109375f, q3 = 0.0112457275390625f,
-              q4 = -0.0004475116729736328f;
+  const float q1 = 0.7890625f, q2 = -0.11572265625f, q3 = 0.01116943359375f, q4 = -0.0004405975341796875f;
   const float az = fabsf(z);
   if (az >= 3.0f) return z > 0.f ? 1.0f : 0.0f;  // 1/2 (1 + 1) or 1/2 (1 - 1)
   const float w = z * z;
