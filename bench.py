@@ -118,6 +118,11 @@ class ClockSampler:
                                          stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
+            # nvidia-smi's start-up (driver queries) is kept out of the timed
+            # region: the region starts once the first sample has arrived
+            t0 = time.perf_counter()
+            while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 5.0:
+                time.sleep(0.01)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
