@@ -13,9 +13,9 @@
 // (blockIdx.z selects the split-K range); the narrow tile doubles the CTAs of
 // the training step's small GEMMs and halves each thread's epilogue, which
 // bounds their latency. Per 32-wide K step the threads stage both operand
-// tiles into shared memory in the canonical K-major core-matrix layout (a
-// transposed operand is scattered as 32-bit pairs while staging, so every MMA
-// reads the layout the inference kernel uses), and one thread issues two
+// tiles into shared memory with 16-byte stores, a K-major operand in the
+// canonical K-major core-matrix layout and a transposed one in the canonical
+// MN-major layout (read with the MMA's transpose bit), and one thread issues two
 // tcgen05.mma (M = 128, N = 32, K = 16) into the 32 accumulator columns and
 // commits them to the stage's mbarrier; two stages alternate, and
 // the global loads of step t + 1 are in flight while step t is staged and its
@@ -80,19 +80,36 @@ static_assert(sizeof(GemmSmem) <= kSmemBytes && kSmemBytes <= 48 * 1024, "GEMM s
 // One operand's rows x BK tile at (r0, k0), held in registers between its
 // global loads and its shared-memory stores, so the loads of step t + 1 are
 // in flight while step t is staged and its MMAs issue. KMAJOR: element (r, k)
-// at src[r * ld + k], else at src[k * ld + r]. Rows >= rows_live are loaded
-// when the stored row is long enough (their results are masked); columns at
-// or past kend are zero. Stores go to the canonical K-major layout.
+// at src[r * ld + k], staged in the canonical K-major layout (core_off);
+// else element (r, k) at src[k * ld + r], staged as it is stored, in the
+// canonical MN-major layout: 16-byte rows of 8 consecutive r at one k, the
+// 8 k of a core matrix 16 bytes apart, core matrices kMnSbo = 128 bytes
+// apart along r and kMnLbo apart along k (the MMA reads it with the
+// operand's transpose bit set). Rows >= rows_live are loaded when the stored
+// row is long enough (their results are masked); k at or past kend is zero.
 template <int ROWS, bool KMAJOR>
 struct OperandTile {
-  // KMAJOR: ROWS x (BK / 8) chunks of 8 k-values; else (BK / 2) x (ROWS / 8)
-  // pairs of chunks (rows k, k + 1 of 8 row-values each)
-  static constexpr int kItems = KMAJOR ? ROWS * (BK / 8) : (BK / 2) * (ROWS / 8);
+  static constexpr int kItems = ROWS * (BK / 8);  // 16-byte chunks
   static constexpr int kPer = (kItems + THREADS - 1) / THREADS;
   static_assert(kItems % THREADS == 0 || kPer == 1, "operand tile items per thread");
+  static constexpr uint32_t kMnSbo = 128;
+  static constexpr uint32_t kMnLbo = uint32_t(ROWS / 8) * 128;
   // threads past the last item (kItems < THREADS) load and store nothing
   static __device__ __forceinline__ bool mine(int c) { return kItems % THREADS == 0 || c < kItems; }
-  uint4 v[KMAJOR ? kPer : 2 * kPer];
+  uint4 v[kPer];
+
+  // chunk c -> (row of its first element, k): KMAJOR 8 k-values of row r;
+  // else 8 rows at one k, with k % 8 varying fastest across a warp so that
+  // consecutive threads fill consecutive 16-byte slots of a core matrix
+  static __device__ __forceinline__ void chunk(int c, int& r, int& k) {
+    if (KMAJOR) {
+      r = c / (BK / 8);
+      k = (c % (BK / 8)) * 8;
+    } else {
+      r = ((c / 8) % (ROWS / 8)) * 8;
+      k = (c / (8 * (ROWS / 8))) * 8 + c % 8;
+    }
+  }
 
   __device__ __forceinline__ void load(const bf16* src, long long ld, long long r0, long long rows_live,
                                        long long k0, long long kend) {
@@ -100,22 +117,11 @@ struct OperandTile {
     for (int i = 0; i < kPer; ++i) {
       const int c = threadIdx.x + i * THREADS;
       if (!mine(c)) break;
-      if (KMAJOR) {
-        const int r = c / (BK / 8), kc = (c % (BK / 8)) * 8;
-        v[i] = make_uint4(0, 0, 0, 0);
-        if (r0 + r < rows_live && k0 + kc < kend) v[i] = *reinterpret_cast<const uint4*>(src + (r0 + r) * ld + k0 + kc);
-      } else {
-        // k varies fastest across a warp (spreads the scattered words over
-        // more banks); both rows of a pair are inside or outside the K range
-        // together (it is a multiple of 8)
-        const int kr = (c % (BK / 2)) * 2, rc = (c / (BK / 2)) * 8;
-        v[2 * i] = make_uint4(0, 0, 0, 0);
-        v[2 * i + 1] = v[2 * i];
-        if (r0 + rc < rows_live && k0 + kr < kend) {
-          v[2 * i] = *reinterpret_cast<const uint4*>(src + (k0 + kr) * ld + r0 + rc);
-          v[2 * i + 1] = *reinterpret_cast<const uint4*>(src + (k0 + kr + 1) * ld + r0 + rc);
-        }
-      }
+      int r, k;
+      chunk(c, r, k);
+      v[i] = make_uint4(0, 0, 0, 0);
+      if (r0 + r < rows_live && k0 + k < kend)
+        v[i] = *reinterpret_cast<const uint4*>(KMAJOR ? src + (r0 + r) * ld + k0 + k : src + (k0 + k) * ld + r0 + r);
     }
   }
 
@@ -125,20 +131,17 @@ struct OperandTile {
     for (int i = 0; i < kPer; ++i) {
       const int c = threadIdx.x + i * THREADS;
       if (!mine(c)) break;
-      if (KMAJOR) {
-        const int r = c / (BK / 8), kc = (c % (BK / 8)) * 8;
-        *reinterpret_cast<uint4*>(base + core_off(r, kc, BK)) = v[i];
-      } else {
-        // element k and k + 1 of a row are adjacent in the layout: one 32-bit
-        // word per row of the chunk
-        const int kr = (c % (BK / 2)) * 2, rc = (c / (BK / 2)) * 8;
-        const unsigned short* e0 = reinterpret_cast<const unsigned short*>(&v[2 * i]);
-        const unsigned short* e1 = reinterpret_cast<const unsigned short*>(&v[2 * i + 1]);
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-          *reinterpret_cast<uint32_t*>(base + core_off(rc + q, kr, BK)) = uint32_t(e0[q]) | (uint32_t(e1[q]) << 16);
-      }
+      int r, k;
+      chunk(c, r, k);
+      const uint32_t off = KMAJOR ? core_off(r, k, BK) : uint32_t(r / 8) * kMnSbo + uint32_t(k / 8) * kMnLbo + (k % 8) * 16;
+      *reinterpret_cast<uint4*>(base + off) = v[i];
     }
+  }
+
+  // descriptor of the K = 16 slice kk of the staged tile
+  static __device__ __forceinline__ uint64_t desc(uint32_t tile, int kk) {
+    return KMAJOR ? smem_desc(tile + kk * 256, 128, (BK / 8) * 128)
+                  : smem_desc(tile + uint32_t(2 * kk) * kMnLbo, kMnLbo, kMnSbo);
   }
 };
 
@@ -187,7 +190,8 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
   __syncthreads();
   fence_after_sync();
   const uint32_t tbase = S.tmem_base;
-  constexpr uint32_t ID = idesc_bf16(BM, BN);
+  // transpose bits of kind::f16: A (bit 15) and B (bit 16) MN-major
+  constexpr uint32_t ID = idesc_bf16(BM, BN) | (A_ROW ? 0u : 1u << 15) | (B_NK ? 0u : 1u << 16);
   bool lost = false;
 
   for (int t = 0; t < steps; ++t) {
@@ -215,8 +219,8 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
       const uint32_t as = smem_u32(S.a[buf]), bs = smem_u32(S.b[buf]);
 #pragma unroll
       for (int kk = 0; kk < BK / 16; ++kk)
-        mma_bf16(tbase, smem_desc(as + kk * 256, 128, (BK / 8) * 128), smem_desc(bs + kk * 256, 128, (BK / 8) * 128),
-                 ID, (t > 0 || kk > 0) ? 1u : 0u);
+        mma_bf16(tbase, OperandTile<BM, A_ROW>::desc(as, kk), OperandTile<BN, B_NK>::desc(bs, kk), ID,
+                 (t > 0 || kk > 0) ? 1u : 0u);
       mma_commit(smem_u32(&S.mbar[buf]));
     }
   }
