@@ -376,6 +376,9 @@ int pcgb_gemm_bf16_tc(int a_layout, int b_layout, int epilogue, const void* A, i
   if (K % 8 || lda % 8 || ldb % 8) return fail(PCGB_EINVAL, "K, lda and ldb must be multiples of 8");
   if (epilogue < 0 || epilogue > 4) return fail(PCGB_EINVAL, "unknown epilogue");
   if (!A || !B) return fail(PCGB_EINVAL, "A and B are required");
+  // operands are read in 16-byte chunks
+  if (reinterpret_cast<uintptr_t>(A) % 16 || reinterpret_cast<uintptr_t>(B) % 16)
+    return fail(PCGB_EINVAL, "A and B must be 16-byte aligned");
   // every 16-byte operand chunk a tile reads must lie inside the stored rows:
   // a transposed operand is read in chunks of 8 rows up to the tile's row
   // count rounded to 8

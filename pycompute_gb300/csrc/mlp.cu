@@ -491,6 +491,9 @@ int pcgb_gemm_bf16(int a_layout, int b_layout, int epilogue, const void* A, int6
   if (M < 0 || N < 0 || K < 0) return mlp_fail(PCGB_EINVAL, "negative GEMM size");
   if (K % 8 || lda % 8 || ldb % 8) return mlp_fail(PCGB_EINVAL, "K, lda and ldb must be multiples of 8");
   if (epilogue < 0 || epilogue > 4) return mlp_fail(PCGB_EINVAL, "unknown epilogue");
+  // operands are read in 16-byte chunks
+  if (reinterpret_cast<uintptr_t>(A) % 16 || reinterpret_cast<uintptr_t>(B) % 16)
+    return mlp_fail(PCGB_EINVAL, "A and B must be 16-byte aligned");
   // every 16-byte operand chunk a tile reads must lie inside the stored rows
   const int64_t m8 = (M + 7) / 8 * 8, n8 = (N + 7) / 8 * 8;
   if ((a_layout == 0 && lda < K) || (a_layout != 0 && lda < m8) || (b_layout == 0 && ldb < K) ||

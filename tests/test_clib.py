@@ -151,3 +151,19 @@ def test_mixed_run_refuses_more_than_2_31_chunks_before_any_gpu_work(entry):
     rc = getattr(L, entry)(None, arr, 1, None, 1, 1e-8, 0.25, 0.75, 0.2, 2.0, 64, 0,
                            *([None] if entry == "pcgb_multi_run" else []), None)
     assert rc != -34
+
+
+@pytest.mark.parametrize("entry", ["pcgb_gemm_bf16_tc", "pcgb_gemm_bf16"])
+def test_training_gemms_refuse_misaligned_operands_before_any_gpu_work(entry):
+    """Both training-GEMM entry points read their operands in 16-byte chunks:
+    a pointer off a 16-byte boundary is refused with EINVAL before anything
+    is read or launched (the pointers here point at nothing)."""
+    L = _lib.lib()
+    fake = ctypes.c_void_p
+    err = L.pcgb_gemm_tc_last_error if entry.endswith("_tc") else L.pcgb_mlp_last_error
+    for a, b in ((0x10008, 0x20000), (0x10000, 0x20002)):
+        args = [0, 0, 1, fake(a), 16, fake(b), 16, 64, 8, 16, 0, fake(0x30000), 17, fake(0x40000), 8, None, 0,
+                None, 0]
+        rc = getattr(L, entry)(*args, *([None] if entry.endswith("_tc") else []), None)
+        assert rc == -22, (a, b, rc)
+        assert b"16-byte aligned" in err()
