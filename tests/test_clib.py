@@ -48,24 +48,25 @@ def _compile(gm, M, dt=0, sdt=1):
 
 def test_nvrtc_compiles_ivim_for_sm103a_within_spill_cap():
     """The LM kernels for a shared protocol are built for 6 resident blocks
-    per SM; their spills stay under the 256-byte cap for the fp32-state builds,
-    and a build over the cap (the all-FP64 one) is followed by the uncapped
-    build, which does not spill."""
+    per SM (the warm LM with its check epilogue for 7); their spills stay
+    under the 256-byte cap for the fp32-state builds, and a build over the cap
+    (the all-FP64 one) is followed by the uncapped build, which does not
+    spill. Groups served from the cubin cache print no log."""
     import re
     w = synth.ivim()
     gm = codegen.generate(w.expr, w.pars, w.consts)
     for dt, sdt in ((0, 1), (0, 0), (1, 1)):
         rc, log, err = _compile(gm, w.M, dt, sdt)
         assert rc == 0, err
-        if not log:  # served from the cubin cache
-            continue
-        blocks = log.split("Function properties for pcgb_lm_c1_b1\n")[1:]
-        spills = [int(re.search(r"(\d+) bytes spill stores", b).group(1)) for b in blocks]
-        assert spills, log[:400]
-        if dt == 0:
-            assert spills[0] <= 256, spills
-        if spills[0] > 256:
-            assert len(spills) >= 2 and spills[1] == 0, spills
+        for kernel in ("pcgb_lm_c1_b1", "pcgb_lmw_c1_b1"):
+            blocks = log.split(f"Function properties for {kernel}\n")[1:]
+            if not blocks:  # that group came from the cubin cache
+                continue
+            spills = [int(re.search(r"(\d+) bytes spill stores", b).group(1)) for b in blocks]
+            if dt == 0:
+                assert spills[0] <= 256, (kernel, spills)
+            if spills[0] > 256:
+                assert len(spills) >= 2 and spills[1] == 0, (kernel, spills)
 
 
 def test_ivim16_fit_and_refit_kernels_keep_the_register_cap(tmp_path):
