@@ -193,6 +193,7 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
   // transpose bits of kind::f16: A (bit 15) and B (bit 16) MN-major
   constexpr uint32_t ID = idesc_bf16(BM, BN) | (A_ROW ? 0u : 1u << 15) | (B_NK ? 0u : 1u << 16);
   bool lost = false;
+  int last_issued = -1;  // thread 0: the last K step whose MMAs it committed
 
   for (int t = 0; t < steps; ++t) {
     const int buf = t & 1;
@@ -222,6 +223,7 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
         mma_bf16(tbase, OperandTile<BM, A_ROW>::desc(as, kk), OperandTile<BN, B_NK>::desc(bs, kk), ID,
                  (t > 0 || kk > 0) ? 1u : 0u);
       mma_commit(smem_u32(&S.mbar[buf]));
+      last_issued = t;
     }
   }
   // the last commit covers every MMA of this CTA
@@ -233,9 +235,11 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
   }
   if (lost) {
     if (threadIdx.x == 0) {
-      // MMAs of the lost phase may still complete: wait for them (bounded)
-      // before the tensor memory they write is returned
-      for (int b = 0; b < 2; ++b) (void)mbar_wait(smem_u32(&S.mbar[b]), 0u, kWaitLimit);
+      // MMAs of the lost phase may still complete: wait (bounded) for the
+      // commit of the last step whose MMAs were issued (MMAs complete in
+      // issue order) before the tensor memory they write is returned
+      if (last_issued >= 0)
+        (void)mbar_wait(smem_u32(&S.mbar[last_issued & 1]), uint32_t((last_issued >> 1) & 1), kWaitLimit);
       if (g.status) atomicExch(g.status, 1);
     }
   } else {
