@@ -489,7 +489,21 @@ int pcgb_gemm_bf16_tc(int a_layout, int b_layout, int epilogue, const void* A, i
                       int64_t bias_stride, float* out_f32, int64_t ldo, void* out_bf16, int64_t ldob,
                       const float* zin, int64_t ldz, int* status, void* stream);
 
-/* Last error of pcgb_gemm_bf16_tc on this host thread. */
+/* pcgb_gemm_bf16_tc with its failure path exposed (no reference
+ * counterpart). wait_limit: mbarrier try_wait rounds before a wait for the
+ * tensor cores counts as lost (0 = the default, 2^22). skip_block: a test hook
+ * for that path - the CTA with this linear index (x + gx (y + gy z), -1 =
+ * none) never issues its MMAs, so its first wait runs out with none of its
+ * tensor-core work in flight; the CTA then sets *status to 1, writes none of
+ * its output tile, still frees its tensor memory, and the call returns
+ * normally. */
+int pcgb_gemm_bf16_tc_ex(int a_layout, int b_layout, int epilogue, const void* A, int64_t lda, const void* B,
+                         int64_t ldb, int64_t M, int64_t N, int64_t K, int64_t k_split, const float* bias,
+                         int64_t bias_stride, float* out_f32, int64_t ldo, void* out_bf16, int64_t ldob,
+                         const float* zin, int64_t ldz, int* status, unsigned wait_limit, int64_t skip_block,
+                         void* stream);
+
+/* Last error of pcgb_gemm_bf16_tc and pcgb_gemm_bf16_tc_ex on this host thread. */
 const char* pcgb_gemm_tc_last_error(void);
 
 /* Mean-squared-error gradient dy = 2 (y - t) / (batch * nout) (bf16, zero in

@@ -105,6 +105,9 @@ SIGNATURES = {
     "pcgb_gemm_bf16_tc": (c_int, [c_int, c_int, c_int, c_void_p, c_i64, c_void_p, c_i64, c_i64, c_i64, c_i64,
                                   c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p,
                                   c_void_p]),
+    "pcgb_gemm_bf16_tc_ex": (c_int, [c_int, c_int, c_int, c_void_p, c_i64, c_void_p, c_i64, c_i64, c_i64, c_i64,
+                                     c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64, c_void_p, c_i64,
+                                     c_void_p, ctypes.c_uint, c_i64, c_void_p]),
     "pcgb_gemm_tc_last_error": (c_char_p, []),
     "pcgb_mlp_mse_grad": (c_int, [c_void_p, c_void_p, c_i64, c_i64, c_int, c_int, c_void_p, c_i64, c_void_p,
                                   c_void_p]),

@@ -67,6 +67,8 @@ struct TcGemmArgs {
   const float* zin;
   long long ldz;
   int* status;
+  unsigned wait_limit;   // try_wait rounds before a wait counts as lost
+  long long skip_block;  // failure-path test: this CTA never issues its first K step (-1 = none)
 };
 
 struct __align__(1024) GemmSmem {
@@ -199,7 +201,7 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
     const int buf = t & 1;
     // the MMAs of step t - 2 read this buffer: wait for their commit
     if (t >= 2) {
-      const bool ok = threadIdx.x != 0 || mbar_wait(smem_u32(&S.mbar[buf]), uint32_t(((t - 2) >> 1) & 1), kWaitLimit);
+      const bool ok = threadIdx.x != 0 || mbar_wait(smem_u32(&S.mbar[buf]), uint32_t(((t - 2) >> 1) & 1), g.wait_limit);
       if (__syncthreads_or(!ok)) {
         lost = true;
         break;
@@ -215,7 +217,14 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
     fence_async_smem();  // staged operands -> visible to the tensor cores
     fence_before_sync();
     __syncthreads();
-    if (threadIdx.x == 0) {
+    // failure-path test: the CTA never issues nor commits its MMAs, so its
+    // first wait on an mbarrier phase runs out while none of its tensor-core
+    // work is in flight
+    const bool skip = g.skip_block >= 0 && (long long)blockIdx.x +
+                                                   (long long)gridDim.x *
+                                                       (blockIdx.y + (long long)gridDim.y * blockIdx.z) ==
+                                               g.skip_block;
+    if (threadIdx.x == 0 && !skip) {
       fence_after_sync();
       const uint32_t as = smem_u32(S.a[buf]), bs = smem_u32(S.b[buf]);
 #pragma unroll
@@ -230,7 +239,7 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
   if (!lost && steps > 0) {
     const int last = steps - 1;
     const bool ok = threadIdx.x != 0 ||
-                    mbar_wait(smem_u32(&S.mbar[last & 1]), uint32_t((last >> 1) & 1), kWaitLimit);
+                    mbar_wait(smem_u32(&S.mbar[last & 1]), uint32_t((last >> 1) & 1), g.wait_limit);
     lost = __syncthreads_or(!ok);
   }
   if (lost) {
@@ -239,7 +248,7 @@ __global__ void __launch_bounds__(THREADS) gemm_tc_kernel(const TcGemmArgs g) {
       // commit of the last step whose MMAs were issued (MMAs complete in
       // issue order) before the tensor memory they write is returned
       if (last_issued >= 0)
-        (void)mbar_wait(smem_u32(&S.mbar[last_issued & 1]), uint32_t((last_issued >> 1) & 1), kWaitLimit);
+        (void)mbar_wait(smem_u32(&S.mbar[last_issued & 1]), uint32_t((last_issued >> 1) & 1), g.wait_limit);
       if (g.status) atomicExch(g.status, 1);
     }
   } else {
@@ -375,6 +384,15 @@ int pcgb_gemm_bf16_tc(int a_layout, int b_layout, int epilogue, const void* A, i
                       int64_t ldb, int64_t M, int64_t N, int64_t K, int64_t k_split, const float* bias,
                       int64_t bias_stride, float* out_f32, int64_t ldo, void* out_bf16, int64_t ldob,
                       const float* zin, int64_t ldz, int* status, void* stream) {
+  return pcgb_gemm_bf16_tc_ex(a_layout, b_layout, epilogue, A, lda, B, ldb, M, N, K, k_split, bias, bias_stride,
+                              out_f32, ldo, out_bf16, ldob, zin, ldz, status, 0u, -1, stream);
+}
+
+int pcgb_gemm_bf16_tc_ex(int a_layout, int b_layout, int epilogue, const void* A, int64_t lda, const void* B,
+                         int64_t ldb, int64_t M, int64_t N, int64_t K, int64_t k_split, const float* bias,
+                         int64_t bias_stride, float* out_f32, int64_t ldo, void* out_bf16, int64_t ldob,
+                         const float* zin, int64_t ldz, int* status, unsigned wait_limit, int64_t skip_block,
+                         void* stream) {
   g_err.clear();
   if (M < 0 || N < 0 || K < 0) return fail(PCGB_EINVAL, "negative GEMM size");
   if (K % 8 || lda % 8 || ldb % 8) return fail(PCGB_EINVAL, "K, lda and ldb must be multiples of 8");
@@ -408,7 +426,8 @@ int pcgb_gemm_bf16_tc(int a_layout, int b_layout, int epilogue, const void* A, i
   if ((N + BN - 1) / BN > 0x7fffffffLL || (M + BM - 1) / BM > 65535 || splits > 65535)
     return fail(PCGB_ERANGE, "GEMM grid too large");
   TcGemmArgs g{static_cast<const bf16*>(A), lda, static_cast<const bf16*>(B), ldb, M, N, K, k_split,
-               bias, bias_stride, out_f32, ldo, static_cast<bf16*>(out_bf16), ldob, zin, ldz, status};
+               bias, bias_stride, out_f32, ldo, static_cast<bf16*>(out_bf16), ldob, zin, ldz, status,
+               wait_limit ? wait_limit : kWaitLimit, skip_block};
   dim3 grid(unsigned((N + BN - 1) / BN), unsigned((M + BM - 1) / BM), unsigned(splits));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e;

@@ -238,6 +238,54 @@ def test_polynomial_gelu_matches_oracle_bit_for_bit():
     assert not np.array_equal(mo.gelu(z, col=6), mo.gelu(z, col=0))
 
 
+@pytest.mark.parametrize("K", [16, 64, 128])
+def test_tcgen05_gemm_lost_wait_sets_status_frees_tmem_and_returns(K):
+    """The failure path of the tcgen05 training GEMM, made to run without any
+    fault: through pcgb_gemm_bf16_tc_ex, CTA 0 (output rows 0-127, columns
+    0-31) never issues its MMAs nor their commits, so its first mbarrier wait
+    - the buffer reuse at K step 2, or the final wait for one and two K steps
+    (K = 16, 64) - never completes while none of its tensor-core work is in
+    flight. With a short wait limit the wait runs out: the call returns
+    normally, the status word reads 1, CTA 0's tile is not written and every
+    other tile equals the mma.sync GEMM. A normal call right after it equals
+    the mma.sync GEMM everywhere, which it could not if the failed CTA had
+    not freed its tensor memory."""
+    M, N = 1000, 136
+    rng = np.random.default_rng(K)
+    A = mo.bf16(rng.standard_normal((M, K)) * 0.3)
+    Bm = mo.bf16(rng.standard_normal((K, N)) * 0.3)
+    ta = torch.from_numpy(np.ascontiguousarray(A)).to(DEV, torch.bfloat16)
+    tb = torch.from_numpy(np.ascontiguousarray(Bm.T)).to(DEV, torch.bfloat16)
+    bias = torch.from_numpy(rng.standard_normal(N).astype(np.float32)).to(DEV)
+    net = WarmStartMLP(16, 4, [0, 1, 2, 2], [0] * 4, [1] * 4, DEV)
+    net.gemm_impl = "mma"
+    want = torch.zeros((M, N), device=DEV)
+    net._gemm(0, 0, 1, ta, K, tb, K, M, N, K, bias=ctypes.c_void_p(bias.data_ptr()), bias_stride=1, out_f32=want,
+              ldo=N)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = torch.full((M, N), -7.0, device=DEV)
+    status = torch.zeros(1, dtype=torch.int32, device=DEV)
+    rc = _lib.lib().pcgb_gemm_bf16_tc_ex(0, 0, 1, p(ta), K, p(tb), K, M, N, K, 0, p(bias), 1, p(out), N, None, 0,
+                                         None, 0, p(status), 1 << 10, 0, stream)
+    _lib.check("pcgb_gemm_bf16_tc_ex", rc)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 1
+    got, ref = out.cpu().numpy(), want.cpu().numpy()
+    assert np.all(got[:128, :32] == -7.0)
+    mask = np.ones((M, N), bool)
+    mask[:128, :32] = False
+    assert np.abs(got - ref)[mask].max() <= 1e-5 * np.abs(ref).max()
+    status.zero_()
+    out.fill_(-7.0)
+    rc = _lib.lib().pcgb_gemm_bf16_tc_ex(0, 0, 1, p(ta), K, p(tb), K, M, N, K, 0, p(bias), 1, p(out), N, None, 0,
+                                         None, 0, p(status), 0, -1, stream)
+    _lib.check("pcgb_gemm_bf16_tc_ex", rc)
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    assert np.abs(out.cpu().numpy() - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
 def test_tcgen05_lost_wait_sets_status_frees_tmem_and_returns():
     """The failure path of the tcgen05 network kernel, made to run without any
     fault: through pcgb_mlp_forward_tc_ex, the issuing thread of the warpgroup
