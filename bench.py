@@ -119,7 +119,8 @@ class ClockSampler:
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
             # nvidia-smi's start-up (driver queries) is kept out of the timed
-            # region: the region starts once the first sample has arrived
+            # region: the caller's work starts once the first sample has
+            # arrived, and callers enter the sampler before their warm-up
             t0 = time.perf_counter()
             while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 5.0:
                 time.sleep(0.01)
@@ -561,15 +562,17 @@ def warm_headline(args, ws, rank, local, dev):
 
     # ---- timed: warm-start steps, device resident --------------------------
     stream = torch.cuda.current_stream()
-    for _ in range(args.warmup):
-        run_warm(k_warm)
-    torch.cuda.synchronize()
-    if ws > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
     step_events = []
     t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # the sampler runs from before the warm-up steps, so its start-up is over
+    # before the timed steps begin
     with ClockSampler(local) as clk:
+        for _ in range(args.warmup):
+            run_warm(k_warm)
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
         torch.cuda.nvtx.range_push("warm_steps")  # lets a profiler select the timed launches
         t_start.record(stream)
         for _ in range(args.steps):
@@ -641,18 +644,38 @@ def warm_headline(args, ws, rank, local, dev):
         return wf.fit_stream([(data_h, outs[i % 2]) for i in range(k)], iters_warm=k_warm, iters_fallback=k_fb,
                              lam0=lam0)
 
-    e2e_steps(max(2, args.warmup))
-    torch.cuda.synchronize()
-    if ws > 1:
-        dist.barrier()
     e_start, e_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(local) as e2e_clk:
+    with ClockSampler(local) as e2e_clk:  # started before the warm-up volumes (see the device steps)
+        e2e_steps(max(2, args.warmup))
+        torch.cuda.synchronize()
+        if ws > 1:
+            dist.barrier()
         e_start.record(stream)
         e2e_steps(args.steps)
         e_end.record(stream)
         torch.cuda.synchronize()
     e2e_ms = max_over_ranks([e_start.elapsed_time(e_end) / args.steps], device=dev)[0]
     e2e_same = bool(torch.equal(outs[(args.steps - 1) % 2], warm_pars_h))
+    # the host link's own rates right after the timed region (copies alone,
+    # nothing else running): the end-to-end step is bound by them when they
+    # exceed the fit (the link is shared with the machine's other GPUs)
+    link = {}
+    dbuf = torch.empty_like(data)
+    for name, fn, nbytes in (("h2d_gbs", lambda: dbuf.copy_(data_h, non_blocking=True), data_h.nbytes),
+                             ("d2h_gbs", lambda: outs[0].copy_(pars, non_blocking=True), outs[0].nbytes)):
+        fn()
+        torch.cuda.synchronize()
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        for _ in range(3):
+            fn()
+        l1.record(stream)
+        torch.cuda.synchronize()
+        link[name] = 3 * nbytes / (l0.elapsed_time(l1) / 1e3) / 1e9
+    # the two directions run at the same time in the stream
+    link["h2d_ms_per_step"] = data_h.nbytes / link["h2d_gbs"] / 1e6
+    link["d2h_ms_per_step"] = outs[0].nbytes / link["d2h_gbs"] / 1e6
+    del dbuf
     # one volume on its own, streamed in chunks (WarmStartFitter.fit_host)
     wf.fit_host(data_h, outs[0], iters_warm=k_warm, iters_fallback=k_fb, lam0=lam0, chunks=args.e2e_chunks)
     torch.cuda.synchronize()
@@ -666,7 +689,7 @@ def warm_headline(args, ws, rank, local, dev):
 
     return {
         "N": N, "step_ms": step_ms, "plain_ms": plain_ms, "e2e_ms": e2e_ms, "lm_ms": lm_ms, "net_ms": net_ms,
-        "e2e_single_ms": e2e_single_ms,
+        "e2e_single_ms": e2e_single_ms, "host_link": link,
         "stages": stages, "clocks": clk.summary(), "e2e_clocks": e2e_clk.summary(), "h2d": data_h.nbytes,
         "d2h": outs[0].nbytes,
         "k_warm": k_warm, "k_plain": k_plain, "e2e_same": e2e_same, "e2e_chunks": args.e2e_chunks,
@@ -1122,7 +1145,7 @@ def main():
                     "d2h_bytes_per_step": h["d2h"], "ms_per_step": h["e2e_ms"],
                     "api": "WarmStartFitter.fit_stream: the timed steps as a sequence of pinned host volumes, "
                            "each copied in and back, copies overlapped with the neighbouring steps' fits",
-                    "matches_device_run": h["e2e_same"], "clocks": h["e2e_clocks"],
+                    "matches_device_run": h["e2e_same"], "clocks": h["e2e_clocks"], "host_link": h["host_link"],
                     "single_volume": {"value": ws * N / (h["e2e_single_ms"] / 1e3), "ms_per_step": h["e2e_single_ms"],
                                       "api": f"WarmStartFitter.fit_host, {h['e2e_chunks']} chunks"}},
             "roofline": {"bound": "hbm", "achieved": lm_gbs, "peak": hbm, "unit": "GB/s", "frac": lm_gbs / hbm,
