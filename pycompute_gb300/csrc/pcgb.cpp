@@ -131,6 +131,13 @@ constexpr int kLmMinBlocks = 6;
 // epilogue per voxel gain from one more block (IVIM-16, 16.7 M voxels, whole
 // warm step: 6 blocks 8.40 ms, 7 blocks 8.30 ms, 8 blocks 8.35 ms)
 constexpr int kLmWarmMinBlocks = 7;
+// the refit of the flagged voxels with the select as its epilogue (group 3):
+// 6, 7 and 8 blocks measured within 0.3 % on the whole warm step (8.32, 8.32,
+// 8.34 ms)
+constexpr int kLmRefitMinBlocks = 6;
+constexpr int lm_min_blocks_of(int g) {
+  return g == 1 ? 0 : (g == 4 ? kLmWarmMinBlocks : (g == 3 ? kLmRefitMinBlocks : kLmMinBlocks));
+}
 constexpr int kLmMaxThreads = 128;
 // Spilled words stay in L1 and cost less than the occupancy gain up to a few
 // hundred bytes per thread (measured with the sample loops rolled, 8.4 M
@@ -407,7 +414,7 @@ int get_cubin(const char* model_source, const char* model_struct, int nparam, in
 // with the LM kernels' occupancy hint, again without it if any of them spills
 // (local memory in use).
 int load_group(pcgb_fitter* ft, int g) {
-  const int tries[2] = {g == 1 ? 0 : (g == 4 ? kLmWarmMinBlocks : kLmMinBlocks), 0};
+  const int tries[2] = {lm_min_blocks_of(g), 0};
   for (int t = 0; t < 2; ++t) {
     if (t == 1 && tries[0] == 0) break;
     std::vector<char> cubin;
@@ -552,7 +559,7 @@ int pcgb_fitter_compile(const char* model_source, const char* model_struct, int 
     std::vector<char> cubin;
     std::string log;
     if (int rc = get_cubin(model_source, model_struct, nparam, nconst, ndata, dtype, solve_dtype, cache_dir, g,
-                           g == 1 ? 0 : (g == 4 ? kLmWarmMinBlocks : kLmMinBlocks), cubin, log))
+                           lm_min_blocks_of(g), cubin, log))
       return rc;
     // the register-capped LM kernels spill too much for this model: the
     // runtime will load the uncapped build, so compile (and cache) it too
