@@ -41,6 +41,14 @@ def _stream():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
+def adam_step_constants(step0: int, total: int, b1: float = 0.9, b2: float = 0.999) -> torch.Tensor:
+    """(total, 3) float32 rows for the training steps step0 + 1 .. step0 + total:
+    Adam's bias corrections 1 - b1^s and 1 - b2^s and the cosine-decay scale
+    (1 + cos(pi i / total)) / 2 of the i-th step of the run."""
+    return torch.tensor([[1 - b1 ** (step0 + 1 + i), 1 - b2 ** (step0 + 1 + i), 0.5 * (1.0 + np.cos(np.pi * i / total))]
+                         for i in range(total)], dtype=torch.float32)
+
+
 @dataclass
 class _Layer:
     fan_in: int
@@ -244,9 +252,7 @@ class WarmStartMLP:
             # per step: Adam's two bias corrections and the cosine-decay scale,
             # made once and read from device memory (no host copy per step, so
             # the host queues steps ahead of the device)
-            steps = [self.step + 1 + i for i in range(total)]
-            corr_tab = torch.tensor([[1 - b1 ** s, 1 - b2 ** s, 0.5 * (1.0 + np.cos(np.pi * i / total))]
-                                     for i, s in enumerate(steps)], dtype=torch.float32).to(self.device)
+            corr_tab = adam_step_constants(self.step, total, b1, b2).to(self.device)
             done = 0
             for ep in range(epochs):
                 for b in range(nb):

@@ -217,3 +217,18 @@ def test_oracle_lockstep_with_reference_host_build():
     assert rep["mismatch_resolved_total"] == 0, rep
     assert rep["min_same_step_code"] >= 0.95, rep
     assert rep["params_within_1e-5_resolved"] >= 0.995, rep
+
+
+def test_adam_step_constants_table():
+    """The per-step Adam constants the training graph reads from device
+    memory: bias corrections 1 - b^s for the run's global step numbers and a
+    cosine decay from 1 toward 0 over the run, rounded to float32 as the
+    per-step host copies it replaces rounded them."""
+    from pycompute_gb300.warmstart import adam_step_constants
+    t = adam_step_constants(5, 4, 0.9, 0.999).numpy()
+    assert t.shape == (4, 3) and t.dtype == np.float32
+    for i in range(4):
+        s = 5 + 1 + i
+        want = np.array([1 - 0.9 ** s, 1 - 0.999 ** s, 0.5 * (1.0 + np.cos(np.pi * i / 4))]).astype(np.float32)
+        assert np.array_equal(t[i], want)
+    assert t[0, 2] == 1.0 and 0.0 < t[-1, 2] < 0.2
